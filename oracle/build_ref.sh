@@ -1,0 +1,24 @@
+#!/usr/bin/env bash
+# Builds the reference's own CPU kernel (pybind11 module `kernel`) from its unmodified
+# sources under /root/reference, with the stand-in headers in oracle/ref_shim/ placed
+# first on the include path. Output goes only to oracle/_ref/ (git-ignored).
+# Needs pybind11 and the Python headers; when either is missing the build is skipped.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${HPDEX_REFERENCE_ROOT:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -f "$REF/src/cpp/mannwhitneyu.cpp" ]; then
+  echo "build_ref: reference sources not present; skipped"; exit 0
+fi
+PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')"
+PB11="$(python3 -c 'import pybind11; print(pybind11.get_include())' 2>/dev/null || true)"
+if [ -z "$PB11" ] || [ ! -f "$PYINC/Python.h" ]; then
+  echo "build_ref: pybind11 or Python headers missing; skipped"; exit 0
+fi
+SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
+mkdir -p "$OUT"
+g++ -O3 -std=c++17 -fopenmp -shared -fPIC \
+  -I"$HERE/ref_shim" -I"$REF/src/cpp/include" -I"$PYINC" -I"$PB11" \
+  "$REF/src/cpp/module.cpp" "$REF/src/cpp/mannwhitneyu.cpp" \
+  -o "$OUT/kernel$SUFFIX"
+echo "build_ref: built $OUT/kernel$SUFFIX"

@@ -1,0 +1,73 @@
+"""Pins the CPU oracle (oracle/mwu_oracle.c) to the reference's own outputs.
+
+Every fixture under tests/golden/ was produced by the reference's compiled kernel
+(AI4Cell/hpdex src/cpp/module.cpp + mannwhitneyu.cpp, built by oracle/build_ref.sh) on the
+stored inputs; the oracle must reproduce U1 and P bit for bit, the same error text, and the
+group means of both summation modes exactly.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_reference_fixture(name, oracle_lib):
+    g = load_golden(name)
+    o = g["options"]
+    args = (g["data"], g["indices"], g["indptr"], g["group_id"], g["n_targets"])
+    if g["error"]:
+        with pytest.raises(RuntimeError) as e:
+            oracle_lib.mannwhitneyu(*args, tie_correction=o["tie_correction"],
+                                    use_continuity=o["use_continuity"],
+                                    zero_handling=o["zero_handling"],
+                                    alternative=o["alternative"], method=o["method"], threads=2)
+        assert str(e.value) == g["error"]
+    else:
+        U1, P = oracle_lib.mannwhitneyu(*args, tie_correction=o["tie_correction"],
+                                        use_continuity=o["use_continuity"],
+                                        zero_handling=o["zero_handling"],
+                                        alternative=o["alternative"], method=o["method"],
+                                        threads=2)
+        np.testing.assert_array_equal(U1, g["U1"])
+        np.testing.assert_array_equal(P, g["P"])
+    G = g["n_targets"] + 1
+    for include_zeros, sfx in ((True, ""), (False, "_nz")):
+        plain = oracle_lib.group_mean(*args[:4], G, include_zeros, 2, False)
+        kahan = oracle_lib.group_mean(*args[:4], G, include_zeros, 2, True)
+        np.testing.assert_array_equal(plain, g["mean_plain" + sfx])
+        np.testing.assert_array_equal(kahan, g["mean_kahan" + sfx])
+
+
+def test_oracle_asymptotic_matches_scipy(oracle_lib):
+    """FP64 scipy semantics (scipy.stats.mannwhitneyu on float64 copies) for the three
+    alternatives with and without continuity, on the small_float fixture's genes."""
+    stats = pytest.importorskip("scipy.stats")
+    g = load_golden("small_float")
+    import scipy.sparse as sp
+    X = sp.csc_matrix((g["data"], g["indices"], g["indptr"]),
+                      shape=(g["group_id"].size, g["indptr"].size - 1)).toarray().astype(np.float64)
+    gid = g["group_id"]
+    T = g["n_targets"]
+    for alt_i, alt in enumerate(("less", "greater", "two-sided")):
+        for cont in (False, True):
+            U1, P = oracle_lib.mannwhitneyu(g["data"], g["indices"], g["indptr"], gid, T,
+                                            use_continuity=cont, zero_handling=3,
+                                            alternative=alt_i, threads=2)
+            for c in range(0, X.shape[1], 37):
+                for t in range(1, T + 1):
+                    r = stats.mannwhitneyu(X[gid == 0, c], X[gid == t, c], alternative=alt,
+                                           method="asymptotic", use_continuity=cont)
+                    i = c * T + (t - 1)
+                    assert U1[i] == r.statistic
+                    assert abs(P[i] - r.pvalue) <= 1e-13 * max(r.pvalue, 1e-300)
+
+
+def test_oracle_exact_reference_discrepancy(oracle_lib):
+    """The reference's exact p counts bounded compositions, not the MWU null: for n1=5,
+    n2=4, U=12 its survival is 0.32224 (two-sided 0.64448), while the exact MWU null gives
+    P(U>=12) = 23/63 = 0.365079... (two-sided 0.730158..., what scipy reports)."""
+    sf = oracle_lib.p_exact_reference(12.0, 5, 4)
+    assert abs(sf - 0.32224) < 1e-15
+    from oracle.exact_null import mwu_sf_exact
+    assert abs(2 * mwu_sf_exact(12, 5, 4) - 0.7301587301587301) < 1e-15
