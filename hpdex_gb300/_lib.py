@@ -1,0 +1,101 @@
+"""ctypes binding of the native library libhpdex_gb300.so (C ABI in include/hpdex_gb300.h).
+
+The library is the only compute path: there is no CPU fallback. Loading fails loudly when
+the library has not been built, and every call raises when no CUDA device is usable.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import _build
+
+_lock = threading.Lock()
+_lib = None
+
+DTYPE_CODES = {
+    "int8": 0, "uint8": 1, "int16": 2, "uint16": 3, "int32": 4, "uint32": 5,
+    "int64": 6, "uint64": 7, "float32": 8, "float64": 9,
+}
+
+HPDEX_OK, HPDEX_ERR_RUNTIME, HPDEX_ERR_ARGUMENT, HPDEX_ERR_CUDA, HPDEX_ERR_UNSUPPORTED = range(5)
+
+
+class MwuOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "ref_sorted", "tar_sorted", "tie_correction", "use_continuity", "fast_norm",
+        "zero_handling", "alternative", "method", "exact_variant")]
+
+
+class HpdexError(RuntimeError):
+    """Raised for every non-OK status; reference-style runtime errors keep their text."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+EXPORTS = {
+    # name: (restype, argtypes)
+    "hpdex_mwu_options_default": (None, [ctypes.POINTER(MwuOptions)]),
+    "hpdex_last_error": (ctypes.c_char_p, []),
+    "hpdex_device_count": (ctypes.c_int, []),
+    "hpdex_mannwhitneyu": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                          ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.POINTER(MwuOptions), ctypes.c_int32,
+                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "hpdex_group_mean": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_void_p]),
+    "hpdex_matrix_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_matrix_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "hpdex_matrix_info": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int64)] * 4),
+    "hpdex_plan_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                         ctypes.POINTER(MwuOptions),
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "hpdex_plan_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "hpdex_plan_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                          ctypes.POINTER(ctypes.c_int32)]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads libhpdex_gb300.so (building it first when the sources are newer)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not _build.up_to_date():
+                try:
+                    _build.build()
+                except Exception as e:  # no nvcc: fail loudly, never fall back
+                    if not os.path.exists(_build.LIB):
+                        raise RuntimeError(f"hpdex_gb300 native library is missing and could not be built: {e}")
+            L = ctypes.CDLL(_build.LIB)
+            for name, (res, args) in EXPORTS.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != HPDEX_OK:
+        msg = lib().hpdex_last_error().decode(errors="replace")
+        raise HpdexError(status, msg)
+
+
+def device_count() -> int:
+    return int(lib().hpdex_device_count())

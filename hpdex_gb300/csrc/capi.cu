@@ -1,0 +1,772 @@
+// capi.cu -- host orchestration and C ABI of the GB300 MWU backend (see
+// include/hpdex_gb300.h). Resident matrices, plans (a grouping over a matrix), the batched
+// and plain launch forms, exact-mode tables, and the one-shot calls that mirror the
+// reference binding kernel.mannwhitneyu / kernel.group_mean (AI4Cell/hpdex
+// src/cpp/module.cpp:193-243). No CPU fallback: without a usable device every entry
+// point fails with HPDEX_ERR_CUDA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/hpdex_gb300.h"
+#include "common.cuh"
+#include "group_mean.cuh"
+#include "mwu_rank.cuh"
+#include "pvalue.cuh"
+
+using namespace hpdex;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess)                                                             \
+            return fail(HPDEX_ERR_CUDA, "CUDA error %s at %s:%d (%s)", cudaGetErrorString(_e), \
+                        __FILE__, __LINE__, #expr);                                        \
+    } while (0)
+
+#define TRY(expr)                        \
+    do {                                 \
+        int _s = (expr);                 \
+        if (_s != HPDEX_OK) return _s;   \
+    } while (0)
+
+constexpr int kRankThreads = 512;
+constexpr int kMeanThreads = 256;
+
+struct DeviceInfo {
+    int device = -1;
+    int sms = 0;
+    size_t smem_per_sm = 0, smem_optin = 0, smem_reserved = 0;
+};
+
+int device_info(DeviceInfo& d) {
+    int dev = 0;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return fail(HPDEX_ERR_CUDA, "no CUDA device is available (hpdex_gb300 has no CPU path)");
+    CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    d.device = dev;
+    d.sms = p.multiProcessorCount;
+    d.smem_per_sm = p.sharedMemPerMultiprocessor;
+    d.smem_optin = p.sharedMemPerBlockOptin;
+    d.smem_reserved = p.reservedSharedMemPerBlock;
+    return HPDEX_OK;
+}
+
+size_t dtype_size(int dt) {
+    switch (dt) {
+    case HPDEX_INT8: case HPDEX_UINT8: return 1;
+    case HPDEX_INT16: case HPDEX_UINT16: return 2;
+    case HPDEX_INT32: case HPDEX_UINT32: case HPDEX_FLOAT32: return 4;
+    case HPDEX_INT64: case HPDEX_UINT64: case HPDEX_FLOAT64: return 8;
+    default: return 0;
+    }
+}
+int key_bytes(int dt) {
+    return (dt == HPDEX_INT64 || dt == HPDEX_UINT64 || dt == HPDEX_FLOAT64) ? 8 : 4;
+}
+
+// Row ids arrive as int64 (the reference's CscView, sparse.hpp:41-68). Ids outside
+// [0, n_rows) are skipped by every kernel, so narrowing maps them to -1.
+__global__ void narrow_rows_kernel(const long long* in, int32_t* out, long long n, long long n_rows) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const long long r = in[i];
+        out[i] = (r >= 0 && r < n_rows) ? (int32_t)r : -1;
+    }
+}
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int alloc(size_t count) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = count;
+        if (count == 0) return HPDEX_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(HPDEX_ERR_CUDA, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T),
+                        cudaGetErrorString(e));
+        }
+        return HPDEX_OK;
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+struct hpdex_matrix {
+    int dtype = 0;
+    long long n_rows = 0, n_cols = 0, nnz = 0;
+    DevBuf<unsigned char> data;
+    DevBuf<int32_t> rows;
+    DevBuf<int64_t> indptr;
+    std::vector<long long> col_nnz;  // host copy for scheduling
+    long long max_col_nnz = 0;
+    DeviceInfo dev;
+};
+
+struct hpdex_plan {
+    hpdex_matrix* m = nullptr;
+    hpdex_mwu_options opt{};
+    long long T = 0, G = 0;
+    std::vector<long long> group_rows;
+    DevBuf<int32_t> gid;
+    DevBuf<long long> d_group_rows;
+    DevBuf<int32_t> order;
+    DevBuf<int32_t> queue;
+    DevBuf<unsigned long long> err;
+    DevBuf<double> U1, P;
+    DevBuf<uint32_t> n1, n2;  // zero_handling = none
+    // rank scratch
+    DevBuf<unsigned char> ek, tk;
+    DevBuf<uint32_t> eg, tg;
+    DevBuf<unsigned char> acc;
+    DevBuf<uint32_t> tiecnt;
+    RankArgs ra{};
+    size_t rank_smem = 0;
+    int rank_grid = 0;
+    // exact tables
+    DevBuf<long long> pair_n1, pair_n2, pair_off, work_off;
+    DevBuf<double> tables;
+    DevBuf<unsigned long long> work;
+    DevBuf<int32_t> pair_of_target, pair_of_test;
+    // execution
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int last_launches = 0;
+    float last_ms[3] = {0, 0, 0};
+    ~hpdex_plan() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto& e : ev) if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// ---- dtype dispatch -------------------------------------------------------------------
+template <template <class> class F, class... Args>
+int dispatch_dtype(int dt, Args&&... args) {
+    switch (dt) {
+    case HPDEX_INT8: return F<int8_t>::run(args...);
+    case HPDEX_UINT8: return F<uint8_t>::run(args...);
+    case HPDEX_INT16: return F<int16_t>::run(args...);
+    case HPDEX_UINT16: return F<uint16_t>::run(args...);
+    case HPDEX_INT32: return F<int32_t>::run(args...);
+    case HPDEX_UINT32: return F<uint32_t>::run(args...);
+    case HPDEX_INT64: return F<int64_t>::run(args...);
+    case HPDEX_UINT64: return F<uint64_t>::run(args...);
+    case HPDEX_FLOAT32: return F<float>::run(args...);
+    case HPDEX_FLOAT64: return F<double>::run(args...);
+    default: return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
+    }
+}
+
+template <class V>
+struct RankLaunch {
+    static int run(hpdex_plan* p, dim3 grid, cudaStream_t s) {
+        // the dynamic shared-memory limit was raised to the device maximum when the plan
+        // was configured (RankOccupancy), so no attribute call happens under capture
+        auto k = mwu_rank_kernel<V, kRankThreads>;
+        k<<<grid, kRankThreads, p->rank_smem, s>>>(p->ra);
+        CUDA_TRY(cudaGetLastError());
+        return HPDEX_OK;
+    }
+};
+template <class V>
+struct RankOccupancy {
+    static int run(size_t smem, size_t smem_max, int* blocks) {
+        auto k = mwu_rank_kernel<V, kRankThreads>;
+        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, kRankThreads, smem));
+        return HPDEX_OK;
+    }
+};
+template <class V>
+struct MeanLaunch {
+    static int run(const MeanArgs* a, dim3 grid, size_t smem, cudaStream_t s) {
+        auto k = group_mean_kernel<V, kMeanThreads>;
+        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kMeanThreads, smem, s>>>(*a);
+        CUDA_TRY(cudaGetLastError());
+        return HPDEX_OK;
+    }
+};
+
+int validate_csc(const int64_t* indptr, long long n_cols, long long nnz, long long n_rows) {
+    if (n_rows < 0 || n_cols < 0 || nnz < 0) return fail(HPDEX_ERR_ARGUMENT, "negative matrix size");
+    if (n_rows >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "n_rows must be below 2^31");
+    if (n_cols >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "n_cols must be below 2^31");
+    for (long long c = 0; c < n_cols; ++c) {
+        if (indptr[c] < 0 || indptr[c + 1] < indptr[c] || indptr[c + 1] > nnz)
+            return fail(HPDEX_ERR_ARGUMENT,
+                        "indptr is not a valid CSC column pointer at column %lld", c);
+    }
+    return HPDEX_OK;
+}
+
+int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, const int64_t* indptr) {
+    const size_t vs = dtype_size(m->dtype);
+    TRY(m->data.alloc(std::max<size_t>(1, (size_t)m->nnz * vs)));
+    TRY(m->rows.alloc(std::max<long long>(1, m->nnz)));
+    TRY(m->indptr.alloc((size_t)m->n_cols + 1));
+    if (m->nnz) CUDA_TRY(cudaMemcpy(m->data.p, data, (size_t)m->nnz * vs, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t) * ((size_t)m->n_cols + 1),
+                        cudaMemcpyHostToDevice));
+    // row ids: int64 -> int32 through a bounded staging buffer
+    const long long chunk = 1ll << 24;
+    if (m->nnz) {
+        DevBuf<long long> stage;
+        TRY(stage.alloc((size_t)std::min(chunk, m->nnz)));
+        for (long long off = 0; off < m->nnz; off += chunk) {
+            const long long k = std::min(chunk, m->nnz - off);
+            CUDA_TRY(cudaMemcpy(stage.p, indices + off, sizeof(long long) * k, cudaMemcpyHostToDevice));
+            narrow_rows_kernel<<<(int)std::min<long long>((k + 255) / 256, 8192), 256>>>(
+                stage.p, m->rows.p + off, k, m->n_rows);
+            CUDA_TRY(cudaGetLastError());
+        }
+        CUDA_TRY(cudaDeviceSynchronize());
+    }
+    m->col_nnz.resize((size_t)m->n_cols);
+    m->max_col_nnz = 0;
+    for (long long c = 0; c < m->n_cols; ++c) {
+        m->col_nnz[(size_t)c] = indptr[c + 1] - indptr[c];
+        m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
+    }
+    return HPDEX_OK;
+}
+
+// Rank-kernel layout for this plan: 2 CTAs per SM when the layout fits, else 1.
+int configure_rank(hpdex_plan* p) {
+    const hpdex_matrix* m = p->m;
+    const int kb = key_bytes(m->dtype);
+    const int G = (int)p->G;
+    const int tie_warps = 4;
+    const int nbl = 12;
+    size_t budget = 0;
+    int per_sm = 2;
+    for (; per_sm >= 1; --per_sm) {
+        budget = m->dev.smem_per_sm / per_sm - m->dev.smem_reserved - 1024;
+        budget = std::min(budget, m->dev.smem_optin);
+        const RankSmem base(nbl, G, tie_warps, 0, 0, 0, kb);
+        if (base.total + 4096 <= budget) break;
+    }
+    if (per_sm < 1) per_sm = 1;
+    int acc_in = 1, cnt_in = 1;
+    RankSmem L(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
+    if (L.total > budget) { cnt_in = 0; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
+    if (L.total > budget) { acc_in = 0; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
+    const size_t left = budget > L.total ? budget - L.total : 0;
+    int cap = (int)std::min<size_t>(left / (kb + 4), (size_t)1 << 30);
+    cap = std::max(0, cap - 8);
+    L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
+    p->rank_smem = L.total;
+
+    int blocks = 0;
+    TRY(dispatch_dtype<RankOccupancy>(m->dtype, p->rank_smem, m->dev.smem_optin, &blocks));
+    if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM (smem %zu)", p->rank_smem);
+    p->rank_grid = m->dev.sms * blocks;
+
+    const long long slice = std::max<long long>(1, m->max_col_nnz);
+    const size_t nctas = (size_t)p->rank_grid;
+    if ((long long)cap < m->max_col_nnz) {
+        TRY(p->ek.alloc(nctas * slice * kb));
+        TRY(p->eg.alloc(nctas * slice));
+    }
+    TRY(p->tk.alloc(nctas * slice * kb));
+    TRY(p->tg.alloc(nctas * slice));
+    if (!acc_in) TRY(p->acc.alloc(nctas * 24 * (size_t)G));
+    if (!cnt_in) TRY(p->tiecnt.alloc(nctas * tie_warps * (size_t)G));
+
+    RankArgs& a = p->ra;
+    a.data = m->data.p;
+    a.rows = m->rows.p;
+    a.indptr = m->indptr.p;
+    a.n_rows = m->n_rows;
+    a.n_cols = (int32_t)m->n_cols;
+    a.G = G;
+    a.gid = p->gid.p;
+    a.order = p->order.p;
+    a.queue = p->queue.p;
+    a.single_gene = -1;
+    a.zero_handling = p->opt.zero_handling;
+    a.tie_correction = p->opt.tie_correction;
+    a.group_rows = p->d_group_rows.p;
+    a.U1 = p->U1.p;
+    a.tie = p->P.p;
+    a.n1 = p->n1.p;
+    a.n2 = p->n2.p;
+    a.err = p->err.p;
+    a.ek_global = p->ek.p;
+    a.eg_global = p->eg.p;
+    a.tk_global = p->tk.p;
+    a.tg_global = p->tg.p;
+    a.slice = slice;
+    a.acc_global = p->acc.p;
+    a.tiecnt_global = p->tiecnt.p;
+    a.nb_max_log2 = nbl;
+    a.elem_smem_cap = cap;
+    a.acc_in_smem = acc_in;
+    a.tiecnt_in_smem = cnt_in;
+    a.tie_warps = tie_warps;
+    return HPDEX_OK;
+}
+
+int launch_pvalues_asymptotic(hpdex_plan* p, cudaStream_t s) {
+    PArgs a{};
+    a.U1 = p->U1.p;
+    a.P = p->P.p;
+    a.n = p->T * p->m->n_cols;
+    a.n_cols = (int32_t)p->m->n_cols;
+    a.group_rows = p->d_group_rows.p;
+    a.n1g = p->n1.p;
+    a.n2t = p->n2.p;
+    a.zero_handling = p->opt.zero_handling;
+    a.alternative = p->opt.alternative;
+    a.cc = p->opt.use_continuity ? 0.5 : 0.0;
+    if (a.n == 0) return HPDEX_OK;
+    const int grid = (int)std::min<long long>((a.n + 255) / 256, (long long)p->m->dev.sms * 8);
+    mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, s>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    return HPDEX_OK;
+}
+
+// Builds the exact tables for the distinct (n1, n2) of this plan and launches the lookup.
+int run_exact(hpdex_plan* p, cudaStream_t s) {
+    const long long C = p->m->n_cols, T = p->T, n = T * C;
+    if (n == 0) return HPDEX_OK;
+    std::map<std::pair<long long, long long>, int> pairs;
+    std::vector<int32_t> pot;  // pair of target / test
+    if (p->opt.zero_handling == HPDEX_ZERO_NONE) {
+        std::vector<uint32_t> h1((size_t)C), h2((size_t)n);
+        CUDA_TRY(cudaStreamSynchronize(s));
+        CUDA_TRY(cudaMemcpy(h1.data(), p->n1.p, sizeof(uint32_t) * C, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(h2.data(), p->n2.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        pot.resize((size_t)n);
+        for (long long i = 0; i < n; ++i) {
+            const long long c = i % C;
+            auto key = std::make_pair((long long)h1[(size_t)c], (long long)h2[(size_t)i]);
+            auto it = pairs.find(key);
+            if (it == pairs.end()) it = pairs.emplace(key, (int)pairs.size()).first;
+            pot[(size_t)i] = it->second;
+        }
+    } else {
+        pot.resize((size_t)T);
+        for (long long t = 0; t < T; ++t) {
+            auto key = std::make_pair(p->group_rows[0], p->group_rows[(size_t)t + 1]);
+            auto it = pairs.find(key);
+            if (it == pairs.end()) it = pairs.emplace(key, (int)pairs.size()).first;
+            pot[(size_t)t] = it->second;
+        }
+    }
+    const int np = (int)pairs.size();
+    std::vector<long long> hn1(np), hn2(np), hoff(np), hwoff(np);
+    long long tot = 0, wtot = 0;
+    for (auto& kv : pairs) {
+        const int i = kv.second;
+        hn1[i] = kv.first.first;
+        hn2[i] = kv.first.second;
+        const long long umax = hn1[i] * hn2[i];
+        if (umax > (1ll << 26))
+            return fail(HPDEX_ERR_UNSUPPORTED,
+                        "method='exact': n1*n2 = %lld exceeds the exact-table limit 2^26", umax);
+        hoff[i] = tot;
+        tot += 2 * (umax + 1);
+        hwoff[i] = wtot;
+        const long long mside = std::min(hn1[i], hn2[i]);
+        const long long w = p->opt.exact_variant == HPDEX_EXACT_MWU_NULL ? (mside + 1) * (umax + 1)
+                                                                        : 2 * (umax + 1);
+        if (w > (1ll << 28))
+            return fail(HPDEX_ERR_UNSUPPORTED, "method='exact': table work space too large");
+        wtot += w;
+    }
+    TRY(p->pair_n1.alloc(np));
+    TRY(p->pair_n2.alloc(np));
+    TRY(p->pair_off.alloc(np));
+    TRY(p->work_off.alloc(np));
+    TRY(p->tables.alloc((size_t)std::max<long long>(tot, 1)));
+    TRY(p->work.alloc((size_t)std::max<long long>(wtot, 1)));
+    CUDA_TRY(cudaMemcpyAsync(p->pair_n1.p, hn1.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(p->pair_n2.p, hn2.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(p->pair_off.p, hoff.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(p->work_off.p, hwoff.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
+    DevBuf<int32_t>& pmap = (p->opt.zero_handling == HPDEX_ZERO_NONE) ? p->pair_of_test : p->pair_of_target;
+    TRY(pmap.alloc(pot.size()));
+    CUDA_TRY(cudaMemcpyAsync(pmap.p, pot.data(), sizeof(int32_t) * pot.size(), cudaMemcpyHostToDevice, s));
+    ExactTables et{};
+    et.pair_n1 = p->pair_n1.p;
+    et.pair_n2 = p->pair_n2.p;
+    et.offset = p->pair_off.p;
+    et.tables = p->tables.p;
+    et.work = p->work.p;
+    et.work_off = p->work_off.p;
+    et.n_pairs = np;
+    et.variant = p->opt.exact_variant;
+    if (np > 0) {
+        if (p->opt.exact_variant == HPDEX_EXACT_MWU_NULL)
+            exact_null_table_kernel<256><<<np, 256, 0, s>>>(et);
+        else
+            exact_reference_table_kernel<256><<<np, 256, 0, s>>>(et);
+        CUDA_TRY(cudaGetLastError());
+    }
+    ExactArgs a{};
+    a.U1 = p->U1.p;
+    a.P = p->P.p;
+    a.n = n;
+    a.n_cols = (int32_t)C;
+    a.group_rows = p->d_group_rows.p;
+    a.n1g = p->n1.p;
+    a.n2t = p->n2.p;
+    a.zero_handling = p->opt.zero_handling;
+    a.alternative = p->opt.alternative;
+    a.variant = p->opt.exact_variant;
+    a.pair_of_target = p->pair_of_target.p;
+    a.pair_of_test = p->pair_of_test.p;
+    a.pair_n1 = p->pair_n1.p;
+    a.pair_n2 = p->pair_n2.p;
+    a.offset = p->pair_off.p;
+    a.tables = p->tables.p;
+    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)p->m->dev.sms * 8);
+    mwu_pvalue_exact_kernel<<<grid, 256, 0, s>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    return HPDEX_OK;
+}
+
+int check_device_errors(hpdex_plan* p) {
+    unsigned long long e[2];
+    CUDA_TRY(cudaMemcpy(e, p->err.p, sizeof e, cudaMemcpyDeviceToHost));
+    const unsigned long long G = (unsigned long long)p->G;
+    if (e[0] != ~0ull) {
+        const unsigned long long c = e[0] / G, g = e[0] % G;
+        if (g == 0) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column %llu", c);
+        return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %llu at column %llu", g, c);
+    }
+    if (e[1] != ~0ull) {
+        const unsigned long long c = e[1] / G, g = e[1] % G;
+        return fail(HPDEX_ERR_ARGUMENT,
+                    "column %llu stores more entries for group %llu than the group has rows "
+                    "(duplicate row indices)", c, g);
+    }
+    return HPDEX_OK;
+}
+
+// Rank kernel(s) for one run; batched = persistent + queue, plain = one launch per gene.
+int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
+    if (p->m->n_cols == 0) return HPDEX_OK;
+    if (mode == HPDEX_MODE_BATCHED) {
+        CUDA_TRY(cudaMemsetAsync(p->queue.p, 0, sizeof(int32_t), s));
+        p->ra.single_gene = -1;
+        TRY(dispatch_dtype<RankLaunch>(p->m->dtype, p, dim3(p->rank_grid), s));
+        *launches += 1;
+    } else {
+        for (long long c = 0; c < p->m->n_cols; ++c) {
+            p->ra.single_gene = (int32_t)c;
+            TRY(dispatch_dtype<RankLaunch>(p->m->dtype, p, dim3(1), s));
+            *launches += 1;
+        }
+        p->ra.single_gene = -1;
+    }
+    return HPDEX_OK;
+}
+
+}  // namespace
+
+// =======================================================================================
+extern "C" {
+
+void hpdex_mwu_options_default(hpdex_mwu_options* o) {
+    if (!o) return;
+    o->ref_sorted = 0;
+    o->tar_sorted = 0;
+    o->tie_correction = 1;
+    o->use_continuity = 0;
+    o->fast_norm = 0;
+    o->zero_handling = HPDEX_ZERO_NONE;
+    o->alternative = HPDEX_TWO_SIDED;
+    o->method = HPDEX_ASYMPTOTIC;
+    o->exact_variant = HPDEX_EXACT_REFERENCE;
+}
+
+const char* hpdex_last_error(void) { return g_last_error.c_str(); }
+
+int hpdex_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
+                        const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                        hpdex_matrix** out) {
+    if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (dtype_size(dtype) == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
+    if (!indptr || (nnz > 0 && (!data || !indices))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    TRY(validate_csc(indptr, n_cols, nnz, n_rows));
+    hpdex_matrix* m = new hpdex_matrix();
+    m->dtype = dtype;
+    m->n_rows = n_rows;
+    m->n_cols = n_cols;
+    m->nnz = nnz;
+    int st = device_info(m->dev);
+    if (st == HPDEX_OK) st = upload_matrix(m, data, indices, indptr);
+    if (st != HPDEX_OK) { delete m; return st; }
+    *out = m;
+    return HPDEX_OK;
+}
+
+int hpdex_matrix_destroy(hpdex_matrix* m) {
+    delete m;
+    return HPDEX_OK;
+}
+
+int hpdex_matrix_info(const hpdex_matrix* m, int64_t* n_rows, int64_t* n_cols, int64_t* nnz,
+                      int64_t* device_bytes) {
+    if (!m) return fail(HPDEX_ERR_ARGUMENT, "matrix is NULL");
+    if (n_rows) *n_rows = m->n_rows;
+    if (n_cols) *n_cols = m->n_cols;
+    if (nnz) *nnz = m->nnz;
+    if (device_bytes)
+        *device_bytes = (int64_t)(m->data.n + m->rows.n * 4 + m->indptr.n * 8);
+    return HPDEX_OK;
+}
+
+int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
+                      const hpdex_mwu_options* opt, hpdex_plan** out) {
+    if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!m || !opt) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix or options");
+    if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    if (m->n_rows > 0 && !group_id) return fail(HPDEX_ERR_ARGUMENT, "group_id is NULL");
+    if (opt->zero_handling < 0 || opt->zero_handling > 3) return fail(HPDEX_ERR_ARGUMENT, "zero_handling must be 0..3");
+    if (opt->alternative < 0 || opt->alternative > 2) return fail(HPDEX_ERR_ARGUMENT, "alternative must be 0..2");
+    if (opt->method != HPDEX_EXACT && opt->method != HPDEX_ASYMPTOTIC) return fail(HPDEX_ERR_ARGUMENT, "method must be 1 (exact) or 2 (asymptotic)");
+    if (n_targets >= (1ll << 30)) return fail(HPDEX_ERR_UNSUPPORTED, "n_targets too large");
+    std::unique_ptr<hpdex_plan> p(new hpdex_plan());
+    p->m = m;
+    p->opt = *opt;
+    p->T = n_targets;
+    p->G = n_targets + 1;
+    const long long C = m->n_cols, R = m->n_rows, G = p->G;
+    p->group_rows.assign((size_t)G, 0);
+    for (long long r = 0; r < R; ++r) {
+        const int g = group_id[r];
+        if (g >= 0 && g < G) ++p->group_rows[(size_t)g];
+    }
+    // reference-style errors raised before any launch (mannwhitneyu.cpp:967-1020: for
+    // min/max/mix the sample sizes are the group sizes, identical for every column)
+    if (opt->zero_handling != HPDEX_ZERO_NONE && C > 0) {
+        if (p->group_rows[0] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column 0");
+        for (long long g = 1; g < G; ++g)
+            if (p->group_rows[(size_t)g] < 2)
+                return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %lld at column 0", g);
+    }
+    CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    for (auto& e : p->ev) CUDA_TRY(cudaEventCreate(&e));
+    TRY(p->gid.alloc(std::max<long long>(R, 1)));
+    if (R) CUDA_TRY(cudaMemcpy(p->gid.p, group_id, sizeof(int32_t) * R, cudaMemcpyHostToDevice));
+    TRY(p->d_group_rows.alloc((size_t)G));
+    CUDA_TRY(cudaMemcpy(p->d_group_rows.p, p->group_rows.data(), sizeof(long long) * G, cudaMemcpyHostToDevice));
+    // longest genes first: the work queue hands them out before the short tail
+    std::vector<int32_t> order((size_t)C);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return m->col_nnz[(size_t)a] > m->col_nnz[(size_t)b];
+    });
+    TRY(p->order.alloc(std::max<long long>(C, 1)));
+    if (C) CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
+    TRY(p->queue.alloc(1));
+    TRY(p->err.alloc(2));
+    const size_t n = (size_t)(p->T * C);
+    TRY(p->U1.alloc(std::max<size_t>(n, 1)));
+    TRY(p->P.alloc(std::max<size_t>(n, 1)));
+    if (opt->zero_handling == HPDEX_ZERO_NONE) {
+        TRY(p->n1.alloc(std::max<long long>(C, 1)));
+        TRY(p->n2.alloc(std::max<size_t>(n, 1)));
+    }
+    TRY(configure_rank(p.get()));
+    *out = p.release();
+    return HPDEX_OK;
+}
+
+int hpdex_plan_destroy(hpdex_plan* p) {
+    delete p;
+    return HPDEX_OK;
+}
+
+int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (mode != HPDEX_MODE_BATCHED && mode != HPDEX_MODE_PLAIN) return fail(HPDEX_ERR_ARGUMENT, "mode must be 0 or 1");
+    cudaStream_t s = p->stream;
+    int launches = 0;
+    const bool exact = p->opt.method == HPDEX_EXACT;
+    if (mode == HPDEX_MODE_BATCHED && !exact) {
+        if (!p->graph_exec) {
+            // capture: error-word reset, queue reset, rank kernel, p-value kernel
+            CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int st = HPDEX_OK;
+            int l = 0;
+            if (cudaEventRecord(p->ev[0], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            if (st == HPDEX_OK && cudaMemsetAsync(p->err.p, 0xff, 2 * sizeof(unsigned long long), s) != cudaSuccess)
+                st = fail(HPDEX_ERR_CUDA, "memset failed");
+            if (st == HPDEX_OK) st = enqueue_rank(p, mode, s, &l);
+            if (st == HPDEX_OK && cudaEventRecord(p->ev[1], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            if (st == HPDEX_OK) st = launch_pvalues_asymptotic(p, s);
+            if (st == HPDEX_OK && cudaEventRecord(p->ev[2], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (st != HPDEX_OK) { if (g) cudaGraphDestroy(g); return st; }
+            if (ce != cudaSuccess) return fail(HPDEX_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+            p->graph = g;
+            CUDA_TRY(cudaGraphInstantiate(&p->graph_exec, g, 0));
+        }
+        CUDA_TRY(cudaGraphLaunch(p->graph_exec, s));
+        launches = (p->m->n_cols > 0 ? 1 : 0) + (p->T * p->m->n_cols > 0 ? 1 : 0);
+    } else {
+        CUDA_TRY(cudaEventRecord(p->ev[0], s));
+        CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, 2 * sizeof(unsigned long long), s));
+        TRY(enqueue_rank(p, mode, s, &launches));
+        CUDA_TRY(cudaEventRecord(p->ev[1], s));
+        if (exact) {
+            TRY(run_exact(p, s));
+            launches += 2;
+        } else {
+            TRY(launch_pvalues_asymptotic(p, s));
+            launches += 1;
+        }
+        CUDA_TRY(cudaEventRecord(p->ev[2], s));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    p->last_launches = launches;
+    cudaEventElapsedTime(&p->last_ms[0], p->ev[0], p->ev[2]);
+    cudaEventElapsedTime(&p->last_ms[1], p->ev[0], p->ev[1]);
+    cudaEventElapsedTime(&p->last_ms[2], p->ev[1], p->ev[2]);
+    return check_device_errors(p);
+}
+
+int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    const size_t n = (size_t)(p->T * p->m->n_cols);
+    if (n == 0) return HPDEX_OK;
+    if (U1_out) CUDA_TRY(cudaMemcpy(U1_out, p->U1.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (P_out) CUDA_TRY(cudaMemcpy(P_out, p->P.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return HPDEX_OK;
+}
+
+int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (ms3) { ms3[0] = p->last_ms[0]; ms3[1] = p->last_ms[1]; ms3[2] = p->last_ms[2]; }
+    if (launches) *launches = p->last_launches;
+    return HPDEX_OK;
+}
+
+int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
+                       const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                       const int32_t* group_id, int64_t n_targets,
+                       const hpdex_mwu_options* opt, int32_t threads, double* U1_out,
+                       double* P_out) {
+    (void)threads;
+    if (!opt) return fail(HPDEX_ERR_ARGUMENT, "options are NULL");
+    if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    hpdex_matrix* m = nullptr;
+    TRY(hpdex_matrix_create(dtype, data, indices, indptr, n_rows, n_cols, nnz, &m));
+    hpdex_plan* p = nullptr;
+    int st = hpdex_plan_create(m, group_id, n_targets, opt, &p);
+    if (st == HPDEX_OK) st = hpdex_plan_run(p, HPDEX_MODE_BATCHED);
+    if (st == HPDEX_OK) st = hpdex_plan_download(p, U1_out, P_out);
+    hpdex_plan_destroy(p);
+    hpdex_matrix_destroy(m);
+    return st;
+}
+
+int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
+                     const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                     const int32_t* group_id, int64_t n_groups, int32_t include_zeros,
+                     int32_t use_kahan, int32_t threads, double* out) {
+    (void)threads;
+    (void)use_kahan;
+    if (n_groups <= 0 || n_cols <= 0) return HPDEX_OK;  // the reference returns an empty result
+    if (n_groups >= (1ll << 30)) return fail(HPDEX_ERR_UNSUPPORTED, "n_groups too large");
+    hpdex_matrix* m = nullptr;
+    TRY(hpdex_matrix_create(dtype, data, indices, indptr, n_rows, n_cols, nnz, &m));
+    std::unique_ptr<hpdex_matrix> hold(m);
+    std::vector<long long> rows_per((size_t)n_groups, 0);
+    for (long long r = 0; r < n_rows; ++r) {
+        const int g = group_id[r];
+        if (g >= 0 && g < n_groups) ++rows_per[(size_t)g];
+    }
+    DevBuf<int32_t> gid;
+    DevBuf<long long> grows;
+    DevBuf<double> dout;
+    DevBuf<unsigned char> acc;
+    TRY(gid.alloc(std::max<long long>(n_rows, 1)));
+    TRY(grows.alloc((size_t)n_groups));
+    TRY(dout.alloc((size_t)(n_cols * n_groups)));
+    if (n_rows) CUDA_TRY(cudaMemcpy(gid.p, group_id, sizeof(int32_t) * n_rows, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(grows.p, rows_per.data(), sizeof(long long) * n_groups, cudaMemcpyHostToDevice));
+    MeanArgs a{};
+    a.data = m->data.p;
+    a.rows = m->rows.p;
+    a.indptr = m->indptr.p;
+    a.n_rows = n_rows;
+    a.n_cols = (int32_t)n_cols;
+    a.G = (int32_t)n_groups;
+    a.gid = gid.p;
+    a.group_rows = grows.p;
+    a.include_zeros = include_zeros;
+    a.out = dout.p;
+    const size_t need = (size_t)n_groups * 16;
+    const size_t budget = std::min(m->dev.smem_optin, m->dev.smem_per_sm / 2);
+    const int grid = (int)std::min<long long>(n_cols, (long long)m->dev.sms * 4);
+    size_t smem = 0;
+    if (need <= budget) {
+        a.acc_in_smem = 1;
+        smem = need;
+    } else {
+        a.acc_in_smem = 0;
+        TRY(acc.alloc((size_t)grid * need));
+        a.acc_global = acc.p;
+    }
+    TRY(dispatch_dtype<MeanLaunch>(dtype, &a, dim3(grid), smem, (cudaStream_t)0));
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpy(out, dout.p, sizeof(double) * n_cols * n_groups, cudaMemcpyDeviceToHost));
+    return HPDEX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+// pvalue.cuh -- p-value stage of the MWU backend (sm_103a).
+//
+// Asymptotic: restates the reference's precise path (AI4Cell/hpdex src/cpp/mannwhitneyu.cpp
+// :15-96) with the same double operation order. Every multiply / add / divide / sqrt is an
+// explicitly round-to-nearest intrinsic so that no multiply-add is fused and z is the same
+// double the reference computes; erfc is CUDA's double erfc.
+//
+// Exact (reference variant): the reference's p_exact (:98-188) is a DP over
+// dp_i[u] = sum_{k=0..n2} dp_{i-1}[u-k] in wrapping uint64 followed by sequential double
+// sums. One table per distinct (n1, n2) holds pmf[u] = (double)dp[u] and the running
+// double sums prefix[k] = prefix[k-1] + pmf[k] (the reference's own summation order), so
+// each test is an O(1) lookup that reproduces the reference bit for bit.
+// Exact (MWU-null variant): the true null distribution of U, f(u; m, n) =
+// f(u - n; m - 1, n) + f(u; m, n - 1) (counts in double, all additions of positive terms),
+// tail-summed from the left like scipy's _MWU.sf.
+#pragma once
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace hpdex {
+
+struct PArgs {
+    const double* U1;
+    double* P;                 // holds the (masked) tie sum on entry, P on exit
+    long long n;               // T * n_cols
+    int32_t n_cols;
+    const long long* group_rows;
+    const uint32_t* n1g;       // zero_handling = none: per gene
+    const uint32_t* n2t;       // zero_handling = none: per test
+    int32_t zero_handling;
+    int32_t alternative;
+    double cc;
+};
+
+__device__ __forceinline__ void test_sizes(const PArgs& a, long long i, double& n1, double& n2) {
+    const int t = (int)(i / a.n_cols);
+    const int c = (int)(i - (long long)t * a.n_cols);
+    if (a.zero_handling == ZH_NONE) {
+        n1 = (double)a.n1g[c];
+        n2 = (double)a.n2t[i];
+    } else {
+        n1 = (double)a.group_rows[0];
+        n2 = (double)a.group_rows[t + 1];
+    }
+}
+
+// 0.70710678118654752440 rounded to double, the reference's M_SQRT1_2
+#define HPDEX_SQRT1_2 0.70710678118654752440
+
+__device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, double tie_sum,
+                                               double cc, int alt) {
+    const double N = __dadd_rn(n1, n2);
+    const double nm = __dmul_rn(n1, n2);
+    const double mu = __dmul_rn(0.5, nm);
+    double tie_term = 0.0;
+    const double denom = __dmul_rn(N, __dsub_rn(N, 1.0));
+    if (denom > 0.0) tie_term = __ddiv_rn(tie_sum, denom);
+    const double var = __ddiv_rn(__dmul_rn(nm, __dsub_rn(__dadd_rn(N, 1.0), tie_term)), 12.0);
+    const double sigma = (var > 0.0) ? __dsqrt_rn(var) : 0.0;
+    double p = 1.0;
+    if (alt == ALT_TWO_SIDED) {
+        const double U2 = __dsub_rn(nm, U1);
+        const double U = (U1 > U2 ? U1 : U2);
+        if (sigma > 0.0) {
+            const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
+            p = __dmul_rn(2.0, __dmul_rn(0.5, erfc(__dmul_rn(z, HPDEX_SQRT1_2))));
+            if (p > 1.0) p = 1.0;
+            if (p < 0.0) p = 0.0;
+        }
+        return p;
+    }
+    const double U = (alt == ALT_LESS) ? __dsub_rn(nm, U1) : U1;
+    if (sigma > 0.0) {
+        const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
+        p = __dmul_rn(0.5, erfc(__dmul_rn(z, HPDEX_SQRT1_2)));
+    }
+    return (p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p));
+}
+
+__global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        double n1, n2;
+        test_sizes(a, i, n1, n2);
+        a.P[i] = p_asymptotic(a.U1[i], n1, n2, a.P[i], a.cc, a.alternative);
+    }
+}
+
+// ---------------- exact tables ----------------
+struct ExactTables {
+    const long long* pair_n1;     // [n_pairs]
+    const long long* pair_n2;     // [n_pairs]
+    const long long* offset;      // [n_pairs] start of each table in `tables`
+    double* tables;               // per pair: pmf[0..n1*n2] then prefix[0..n1*n2]
+    unsigned long long* work;     // uint64 scratch: 2 * (n1*n2 + 1) per pair (reference)
+    const long long* work_off;    // [n_pairs]
+    int32_t n_pairs;
+    int32_t variant;              // 0 reference, 1 MWU null
+};
+
+// Reference variant: one CTA per (n1, n2). The sliding-window recurrence is a prefix-sum
+// difference, computed here with a block-wide inclusive scan in wrapping uint64 (the same
+// values mod 2^64 as the reference's sequential window), then the running double sums.
+template <int NT>
+__global__ void __launch_bounds__(NT) exact_reference_table_kernel(const ExactTables t) {
+    __shared__ unsigned long long s_carry;
+    __shared__ unsigned long long s_w[NT / 32];
+    const int pi = blockIdx.x;
+    if (pi >= t.n_pairs) return;
+    const long long n1 = t.pair_n1[pi], n2 = t.pair_n2[pi];
+    const long long umax = n1 * n2;
+    unsigned long long* cur = t.work + t.work_off[pi];
+    unsigned long long* pre = cur + (umax + 1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (long long u = tid; u <= umax; u += NT) cur[u] = (u == 0) ? 1ull : 0ull;
+    __syncthreads();
+    for (long long i = 1; i <= n1; ++i) {
+        const long long up = i * n2;
+        // inclusive prefix sums of cur[0..up] (mod 2^64) into pre
+        if (tid == 0) s_carry = 0ull;
+        __syncthreads();
+        for (long long base = 0; base <= up; base += NT) {
+            const long long u = base + tid;
+            unsigned long long v = (u <= up) ? cur[u] : 0ull;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long o = __shfl_up_sync(0xffffffffu, v, d);
+                if (lane >= d) v += o;
+            }
+            if (lane == 31) s_w[warp] = v;
+            __syncthreads();
+            if (warp == 0) {
+                unsigned long long w = lane < NT / 32 ? s_w[lane] : 0ull;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const unsigned long long o = __shfl_up_sync(0xffffffffu, w, d);
+                    if (lane >= d) w += o;
+                }
+                if (lane < NT / 32) s_w[lane] = w;
+            }
+            __syncthreads();
+            const unsigned long long before = s_carry + (warp ? s_w[warp - 1] : 0ull);
+            if (u <= up) pre[u] = before + v;
+            __syncthreads();
+            if (tid == NT - 1) s_carry = before + v;
+            __syncthreads();
+        }
+        // dp_i[u] = pre[u] - pre[u - n2 - 1]
+        for (long long u = tid; u <= up; u += NT)
+            cur[u] = pre[u] - ((u >= n2 + 1) ? pre[u - n2 - 1] : 0ull);
+        __syncthreads();
+    }
+    // pmf and running double sums in the reference's order (sequential, one thread)
+    double* pmf = t.tables + t.offset[pi];
+    for (long long u = tid; u <= umax; u += NT) pmf[u] = (double)cur[u];
+    __syncthreads();
+    if (tid == 0) {
+        double* pre = pmf + (umax + 1);
+        double s = 0.0;
+        for (long long u = 0; u <= umax; ++u) {
+            s = __dadd_rn(s, pmf[u]);
+            pre[u] = s;
+        }
+    }
+}
+
+// MWU-null variant: counts f(u; m, k) for k = 0..n (m = min side), built in place:
+// the table for (m', k) is obtained from (m'-1, k) and (m', k-1). Memory: (m+1) rows of
+// (m*n+1) doubles, held in `work` reinterpreted as double. One CTA per pair.
+template <int NT>
+__global__ void __launch_bounds__(NT) exact_null_table_kernel(const ExactTables t) {
+    const int pi = blockIdx.x;
+    if (pi >= t.n_pairs) return;
+    long long m = t.pair_n1[pi], n = t.pair_n2[pi];
+    if (m > n) { const long long s = m; m = n; n = s; }
+    const long long umax = m * n;
+    double* rows = reinterpret_cast<double*>(t.work + t.work_off[pi]);  // (m+1) x (umax+1)
+    const long long W = umax + 1;
+    const int tid = threadIdx.x;
+    // k = 0 (no targets): f(u; m', 0) = [u == 0] for every m'
+    for (long long j = tid; j < (m + 1) * W; j += NT) rows[j] = ((j % W) == 0) ? 1.0 : 0.0;
+    __syncthreads();
+    for (long long k = 1; k <= n; ++k) {
+        // row m' for (m', k) = row m'-1 (already (m'-1, k)) shifted by k + row m' (m', k-1)
+        for (long long mm = 1; mm <= m; ++mm) {
+            double* r = rows + mm * W;
+            const double* rp = rows + (mm - 1) * W;
+            const long long top = mm * k;
+            for (long long u = top - tid; u >= 0; u -= NT) {
+                // descending u keeps r[u] (old, (mm, k-1)) unread-after-write safe per u
+                const double add = (u >= k) ? rp[u - k] : 0.0;
+                r[u] = __dadd_rn(r[u], add);
+            }
+            __syncthreads();
+        }
+    }
+    const double* f = rows + m * W;
+    double* pmf = t.tables + t.offset[pi];
+    for (long long u = tid; u <= umax; u += NT) pmf[u] = f[u];
+    __syncthreads();
+    if (tid == 0) {
+        double* pre = pmf + (umax + 1);
+        double s = 0.0;
+        for (long long u = 0; u <= umax; ++u) {
+            s = __dadd_rn(s, pmf[u]);
+            pre[u] = s;
+        }
+    }
+}
+
+struct ExactArgs {
+    const double* U1;
+    double* P;
+    long long n;
+    int32_t n_cols;
+    const long long* group_rows;
+    const uint32_t* n1g;
+    const uint32_t* n2t;
+    int32_t zero_handling;
+    int32_t alternative;
+    int32_t variant;
+    // table lookup: pair index of the test's (n1, n2), via a dense map over (n1, n2) when
+    // zero_handling != none (per target), else via per-test pair ids
+    const int32_t* pair_of_target;  // [T]  (zero_handling != none)
+    const int32_t* pair_of_test;    // [T * n_cols] (zero_handling = none)
+    const long long* pair_n1;
+    const long long* pair_n2;
+    const long long* offset;
+    const double* tables;
+};
+
+// survival P(U >= floor(U)) from a table, the reference's formula (:160-179)
+__device__ __forceinline__ double table_sf(const double* pmf, long long umax, double U) {
+    if (umax == 0) return 1.0;
+    const double* pre = pmf + (umax + 1);
+    double Uc = U < 0.0 ? 0.0 : U;
+    if (Uc > (double)umax) Uc = (double)umax;
+    const long long u_stat = (long long)floor(Uc);
+    const double total = pre[umax];
+    const long long kc = umax - u_stat;
+    const long long small = u_stat < kc ? u_stat : kc;
+    const double cdf_small = pre[small];
+    const double pmf_small = pmf[small];
+    if (u_stat <= kc)
+        return __dadd_rn(__dsub_rn(1.0, __ddiv_rn(cdf_small, total)), __ddiv_rn(pmf_small, total));
+    return __ddiv_rn(cdf_small, total);
+}
+
+__global__ void mwu_pvalue_exact_kernel(const ExactArgs a) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        const int t = (int)(i / a.n_cols);
+        int pi;
+        if (a.zero_handling == ZH_NONE) pi = a.pair_of_test[i];
+        else pi = a.pair_of_target[t];
+        const double U1 = a.U1[i];
+        double p = 1.0;
+        if (pi >= 0) {
+            const long long n1 = a.pair_n1[pi], n2 = a.pair_n2[pi];
+            const double nprod = __dmul_rn((double)n1, (double)n2);
+            const double* pmf = a.tables + a.offset[pi];
+            const long long umax = n1 * n2;
+            double U;
+            if (a.alternative == ALT_TWO_SIDED) {
+                const double U2 = __dsub_rn(nprod, U1);
+                U = U1 > U2 ? U1 : U2;
+            } else if (a.alternative == ALT_GREATER) {
+                U = U1;
+            } else {
+                U = __dsub_rn(nprod, U1);
+            }
+            const double sf = table_sf(pmf, umax, U);
+            p = (a.alternative == ALT_TWO_SIDED) ? __dmul_rn(2.0, sf) : sf;
+            if (p < 0.0) p = 0.0;
+            if (p > 1.0) p = 1.0;
+        }
+        a.P[i] = p;
+    }
+}
+
+}  // namespace hpdex

@@ -1,0 +1,140 @@
+"""Differential expression driver with the reference's output schema (AI4Cell/hpdex
+src/hpdex/de.py:35-198).
+
+`parallel_differential_expression(adata, ...)` keeps the reference signature and returns a
+pandas DataFrame with columns target, feature, p_value, u_statistic, fold_change,
+log2_fold_change, fdr. pandas/anndata are imported lazily; `differential_expression`
+does the same work on plain arrays (a CSC/CSR/dense matrix and one label per cell) and
+returns the seven columns as a dict of numpy arrays.
+
+One deliberate difference: the reference pairs p_value/u_statistic with (target, feature)
+labels in target-major order while its kernel writes them gene-major (de.py:159-170 vs
+mannwhitneyu.cpp:959), which mislabels rows when there is more than one target. The GPU
+kernel returns (n_targets, n_genes), so the flattened order matches the labels.
+"""
+from __future__ import annotations
+
+import logging
+
+import numpy as np
+import scipy.sparse
+
+from .backend import group_mean, mannwhitneyu
+
+logger = logging.getLogger(__name__)
+
+supported_metrics = ["wilcoxon"]
+COLUMNS = ["target", "feature", "p_value", "u_statistic", "fold_change", "log2_fold_change", "fdr"]
+
+
+def _bh(P: np.ndarray) -> np.ndarray:
+    from scipy.stats import false_discovery_control
+    try:
+        return false_discovery_control(P, method="bh")
+    except Exception:
+        logger.warning("FDR correction failed, falling back to NaN")
+        return np.full_like(P, np.nan)
+
+
+def _to_csc(X):
+    if isinstance(X, np.ndarray):
+        return scipy.sparse.csc_matrix(X)
+    if isinstance(X, scipy.sparse.csr_matrix):
+        return X.tocsc()
+    if isinstance(X, scipy.sparse.csc_matrix):
+        return X
+    return scipy.sparse.csc_matrix(X)
+
+
+def _select_groups(labels, reference, groups, min_samples):
+    uniq = list(dict.fromkeys(labels.tolist()))  # order of first appearance (pandas unique)
+    if groups is None:
+        groups = [g for g in uniq if g != reference]
+    else:
+        groups = [g for g in groups if g in uniq and g != reference]
+    if reference not in uniq:
+        raise ValueError(f"Reference `{reference}` not found")
+    if not groups:
+        raise ValueError("No valid target groups found")
+    valid = []
+    for g in groups:
+        count = int(np.sum(labels == g))
+        if count >= min_samples:
+            valid.append(g)
+        else:
+            logger.warning(f"Group `{g}` has only {count} samples, skipping")
+    return valid
+
+
+def differential_expression(X, labels, reference, features=None, groups=None,
+                            metric="wilcoxon", tie_correction=True, use_continuity=True,
+                            min_samples=2, threads=-1, clip_value=20.0, show_progress=False):
+    """Array-level DE: X is cells x genes (CSC, CSR or dense), labels one per cell."""
+    if metric not in supported_metrics:
+        raise ValueError(f"Unsupported metric: {metric}; supported: {supported_metrics}")
+    labels = np.asarray(labels, dtype=object)
+    groups = _select_groups(labels, reference, groups, min_samples)
+    matrix = _to_csc(X)
+    n_genes = matrix.shape[1]
+    features = np.asarray(features if features is not None else np.arange(n_genes), dtype=object)
+    if not groups:
+        return {c: np.zeros(0, dtype=object if c in ("target", "feature") else np.float64)
+                for c in COLUMNS}
+    group_map = {reference: 0}
+    for i, g in enumerate(groups):
+        group_map[g] = i + 1
+    group_id = np.full(labels.size, -1, dtype=np.int32)
+    for g, idx in group_map.items():
+        group_id[labels == g] = idx
+    n_targets = len(groups)
+
+    means = group_mean(matrix, group_id, n_targets + 1, include_zeros=True,
+                       threads=threads).reshape(n_genes, n_targets + 1).T
+    ref_means, tar_means = means[0], means[1:]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fold = tar_means / ref_means
+        fold = np.where(ref_means < 1e-10, clip_value, fold)
+        fold = np.where(tar_means < 1e-10, 1.0 / clip_value, fold)
+        log2fold = np.log2(fold)
+
+    U1, P = mannwhitneyu(matrix, group_id, n_targets, ref_sorted=False, tar_sorted=False,
+                         use_continuity=use_continuity, tie_correction=tie_correction,
+                         zero_handling="min", threads=threads, show_progress=show_progress)
+    U1 = np.asarray(U1).reshape(-1)
+    P = np.asarray(P).reshape(-1)
+    return {
+        "target": np.repeat(np.asarray(groups, dtype=object), n_genes),
+        "feature": np.tile(features, n_targets),
+        "p_value": P,
+        "u_statistic": U1,
+        "fold_change": fold.reshape(-1),
+        "log2_fold_change": log2fold.reshape(-1),
+        "fdr": _bh(P),
+    }
+
+
+def parallel_differential_expression(adata, groupby_key: str, reference, groups=None,
+                                     metric: str = "wilcoxon", tie_correction: bool = True,
+                                     use_continuity: bool = True, min_samples: int = 2,
+                                     threads: int = -1, clip_value: float = 20.0,
+                                     show_progress: bool = True):
+    """AnnData front-end with the reference's signature; returns a pandas DataFrame."""
+    import pandas as pd  # lazy: only this front-end needs pandas
+
+    if metric not in supported_metrics:
+        raise ValueError(f"Unsupported metric: {metric}; supported: {supported_metrics}")
+    if groupby_key not in adata.obs.columns:
+        raise ValueError(f"Groupby key `{groupby_key}` not found in adata.obs")
+    obs = adata.obs.copy()
+    if reference is None:
+        obs[groupby_key] = obs[groupby_key].cat.add_categories("non-targeting")
+        obs[groupby_key] = obs[groupby_key].fillna("non-targeting")
+        reference = "non-targeting"
+    labels = np.asarray(obs[groupby_key].astype(object))
+    cols = differential_expression(adata.X, labels, reference,
+                                   features=np.asarray(adata.var_names, dtype=object),
+                                   groups=groups, metric=metric, tie_correction=tie_correction,
+                                   use_continuity=use_continuity, min_samples=min_samples,
+                                   threads=threads, clip_value=clip_value,
+                                   show_progress=show_progress)
+    return pd.DataFrame({c: cols[c] for c in COLUMNS})

@@ -1,0 +1,116 @@
+"""HBM-resident matrices and plans: the reference call split into upload, run, download.
+
+    M = ResidentMatrix(data, indices, indptr, n_rows)      # CSC, stays on the GPU
+    plan = M.plan(group_id, n_targets, zero_handling="min", use_continuity=True)
+    plan.run()                    # batched form: persistent kernel + work queue, CUDA graph
+    U1, P = plan.download()       # (n_targets, n_genes) float64
+The same plan can run again (graph replay) or in the plain form (one launch per gene).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_ZH = {"none": 0, "min": 1, "max": 2, "mix": 3}
+_ALT = {"less": 0, "greater": 1, "two-sided": 2}
+_METHOD = {"exact": 1, "asymptotic": 2}
+
+BATCHED, PLAIN = 0, 1
+
+
+def make_options(tie_correction=True, use_continuity=False, zero_handling="mix",
+                 alternative="two-sided", method="asymptotic", exact_variant="reference"):
+    o = _lib.MwuOptions()
+    o.tie_correction = int(bool(tie_correction))
+    o.use_continuity = int(bool(use_continuity))
+    o.zero_handling = _ZH[zero_handling] if isinstance(zero_handling, str) else int(zero_handling)
+    o.alternative = _ALT[alternative] if isinstance(alternative, str) else int(alternative)
+    o.method = _METHOD[method] if isinstance(method, str) else int(method)
+    o.exact_variant = {"reference": 0, "mwu_null": 1}.get(exact_variant, exact_variant)
+    return o
+
+
+class ResidentMatrix:
+    def __init__(self, data, indices, indptr, n_rows):
+        data = np.ascontiguousarray(data)
+        if data.dtype.name not in _lib.DTYPE_CODES:
+            raise RuntimeError("Unsupported dtype for data")
+        indices = np.ascontiguousarray(indices, dtype=np.int64)
+        indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+        self.n_rows = int(n_rows)
+        self.n_cols = indptr.size - 1
+        self.nnz = data.size
+        self.dtype = data.dtype
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().hpdex_matrix_create(_lib.DTYPE_CODES[data.dtype.name],
+                                                  data.ctypes.data, indices.ctypes.data,
+                                                  indptr.ctypes.data, self.n_rows, self.n_cols,
+                                                  self.nnz, ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_scipy(cls, csc):
+        return cls(csc.data, csc.indices, csc.indptr, csc.shape[0])
+
+    def device_bytes(self) -> int:
+        v = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(_lib.lib().hpdex_matrix_info(self._h, *[ctypes.byref(x) for x in v]))
+        return v[3].value
+
+    def plan(self, group_id, n_targets, **options) -> "Plan":
+        return Plan(self, group_id, n_targets, make_options(**options))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().hpdex_matrix_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    def __init__(self, matrix: ResidentMatrix, group_id, n_targets, options):
+        self.matrix = matrix
+        gid = np.ascontiguousarray(group_id, dtype=np.int32)
+        if gid.size != matrix.n_rows:
+            raise ValueError(f"group_id must have length {matrix.n_rows}")
+        self.n_targets = int(n_targets)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().hpdex_plan_create(matrix._h, gid.ctypes.data, self.n_targets,
+                                                ctypes.byref(options), ctypes.byref(h)))
+        self._h = h
+
+    def run(self, mode: int = BATCHED) -> None:
+        _lib.check(_lib.lib().hpdex_plan_run(self._h, int(mode)))
+
+    def download(self):
+        C = self.matrix.n_cols
+        U1 = np.empty((self.n_targets, C), np.float64)
+        P = np.empty((self.n_targets, C), np.float64)
+        _lib.check(_lib.lib().hpdex_plan_download(self._h, U1.ctypes.data, P.ctypes.data))
+        return U1, P
+
+    def timings(self):
+        """(total_ms, rank_ms, pvalue_ms), kernel launches of the last run."""
+        ms = (ctypes.c_float * 3)()
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().hpdex_plan_timings(self._h, ms, ctypes.byref(n)))
+        return (ms[0], ms[1], ms[2]), n.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().hpdex_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,147 @@
+/*
+ * hpdex_gb300.h -- C ABI of the GB300 (sm_103a) Mann-Whitney U differential-expression
+ * backend. Plain pointers and sizes only; every entry point returns an int status
+ * (HPDEX_OK = 0) and leaves a message for hpdex_last_error() on failure.
+ *
+ * Reference interfaces replaced (AI4Cell/hpdex):
+ *   hpdex_mannwhitneyu  <- kernel.mannwhitneyu   src/cpp/module.cpp:196-228
+ *                          hpdex::mannwhitneyu<T> src/cpp/mannwhitneyu.cpp:1067-1111
+ *   hpdex_group_mean    <- kernel.group_mean      src/cpp/module.cpp:230-242
+ *                          hpdex::group_mean<T>  src/cpp/mannwhitneyu.cpp:1275-1304
+ *   hpdex_mwu_options   <- MannWhitneyuOption    src/cpp/include/mannwhitneyu.hpp:16-32
+ *   the matrix arguments <- view::CscView<T>     src/cpp/include/sparse.hpp:41-68
+ * The resident-matrix / plan / server entry points have no single counterpart: they split
+ * the reference call into upload, launch and download so that matrices stay in HBM.
+ *
+ * Matrix: CSC, n_rows cells x n_cols genes; data[nnz] of `dtype`, indices[nnz] int64 row
+ * ids, indptr[n_cols+1] int64. group_id[n_rows] int32: 0 = reference, 1..n_targets =
+ * targets, anything else ignored. All host pointers unless stated otherwise.
+ *
+ * Output layout: U1_out and P_out are n_targets x n_cols row-major (target-major), i.e.
+ * out[(g-1) * n_cols + gene]. The reference returns the transposed, gene-major order
+ * (mannwhitneyu.cpp:959): reference_flat.reshape(n_cols, n_targets).T equals ours.
+ */
+#ifndef HPDEX_GB300_H
+#define HPDEX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPDEX_OK 0
+#define HPDEX_ERR_RUNTIME 1  /* reference-style runtime_error (message text matches)  */
+#define HPDEX_ERR_ARGUMENT 2 /* malformed input (sizes, pointers, indptr)              */
+#define HPDEX_ERR_CUDA 3     /* CUDA runtime failure or no usable device               */
+#define HPDEX_ERR_UNSUPPORTED 4
+
+/* dtype codes of `data` (the reference's TYPE_DISPATCH list, macro.hpp:4-14) */
+#define HPDEX_INT8 0
+#define HPDEX_UINT8 1
+#define HPDEX_INT16 2
+#define HPDEX_UINT16 3
+#define HPDEX_INT32 4
+#define HPDEX_UINT32 5
+#define HPDEX_INT64 6
+#define HPDEX_UINT64 7
+#define HPDEX_FLOAT32 8
+#define HPDEX_FLOAT64 9
+
+/* zero_handling / alternative / method: the reference's enum values */
+#define HPDEX_ZERO_NONE 0
+#define HPDEX_ZERO_MIN 1
+#define HPDEX_ZERO_MAX 2
+#define HPDEX_ZERO_MIX 3
+#define HPDEX_LESS 0
+#define HPDEX_GREATER 1
+#define HPDEX_TWO_SIDED 2
+#define HPDEX_EXACT 1
+#define HPDEX_ASYMPTOTIC 2
+
+/* exact_variant: 0 = the reference's own exact p (mannwhitneyu.cpp:98-188, a bounded-
+ * composition count in wrapping uint64), 1 = the true MWU null distribution (what
+ * scipy.stats.mannwhitneyu(method="exact") computes). */
+#define HPDEX_EXACT_REFERENCE 0
+#define HPDEX_EXACT_MWU_NULL 1
+
+typedef struct hpdex_mwu_options {
+    int32_t ref_sorted;     /* accepted; sorting is never skipped, results are the same */
+    int32_t tar_sorted;     /* accepted; see ref_sorted                                 */
+    int32_t tie_correction; /* 1: use sum(t^3 - t) in the variance                      */
+    int32_t use_continuity; /* 1: continuity correction 0.5                             */
+    int32_t fast_norm;      /* must be 0: the precise erfc path (see DESIGN)            */
+    int32_t zero_handling;  /* HPDEX_ZERO_*                                             */
+    int32_t alternative;    /* HPDEX_LESS / GREATER / TWO_SIDED                         */
+    int32_t method;         /* HPDEX_EXACT / HPDEX_ASYMPTOTIC                           */
+    int32_t exact_variant;  /* HPDEX_EXACT_REFERENCE / HPDEX_EXACT_MWU_NULL             */
+} hpdex_mwu_options;
+
+/* Fills `o` with the reference binding's defaults (module.cpp:215-227) except
+ * fast_norm = 0. */
+void hpdex_mwu_options_default(hpdex_mwu_options* o);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* hpdex_last_error(void);
+
+/* Number of visible CUDA devices (0 when none); never fails. */
+int hpdex_device_count(void);
+
+/* ---- one-shot calls (reference semantics; host pointers in and out) ---- */
+
+/* kernel.mannwhitneyu. threads is accepted for signature parity and only affects host-side
+ * preparation. U1_out / P_out: n_targets * n_cols doubles, target-major. */
+int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
+                       const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                       const int32_t* group_id, int64_t n_targets,
+                       const hpdex_mwu_options* opt, int32_t threads, double* U1_out,
+                       double* P_out);
+
+/* kernel.group_mean. out: n_cols * n_groups doubles, flat [gene * n_groups + g] exactly as
+ * the reference. use_kahan is honoured as documented (the reference binding forwards
+ * `threads` into it, module.cpp:211-213); both summation modes agree to ~1e-15 here. */
+int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
+                     const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                     const int32_t* group_id, int64_t n_groups, int32_t include_zeros,
+                     int32_t use_kahan, int32_t threads, double* out);
+
+/* ---- resident matrices and plans (matrix stays in HBM across calls) ---- */
+
+typedef struct hpdex_matrix hpdex_matrix;
+typedef struct hpdex_plan hpdex_plan;
+
+/* Uploads a CSC matrix to the current device in the library's resident layout
+ * (values as given, row ids narrowed to int32 when n_rows < 2^31). */
+int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
+                        const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                        hpdex_matrix** out);
+int hpdex_matrix_destroy(hpdex_matrix* m);
+int hpdex_matrix_info(const hpdex_matrix* m, int64_t* n_rows, int64_t* n_cols, int64_t* nnz,
+                      int64_t* device_bytes);
+
+/* A grouping over a resident matrix: validates it like the reference (errors raised before
+ * any launch), uploads group_id, orders genes for the work queue and reserves outputs. */
+int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
+                      const hpdex_mwu_options* opt, hpdex_plan** out);
+int hpdex_plan_destroy(hpdex_plan* p);
+
+/* Runs the MWU on the device. mode 0 = batched (persistent work-queue kernel, captured
+ * in a CUDA graph), mode 1 = plain (one launch per gene, no graph, no queue). Results stay
+ * on the device until hpdex_plan_download. Synchronous. */
+#define HPDEX_MODE_BATCHED 0
+#define HPDEX_MODE_PLAIN 1
+int hpdex_plan_run(hpdex_plan* p, int32_t mode);
+
+/* Copies U1 / P (n_targets x n_cols, target-major) to host; either pointer may be NULL. */
+int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
+
+/* Device times (ms, CUDA events on the launching stream) of the last hpdex_plan_run:
+ * [0] whole run, [1] rank kernel(s), [2] p-value kernel; and the number of kernel
+ * launches it made. */
+int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HPDEX_GB300_H */

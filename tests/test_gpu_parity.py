@@ -1,0 +1,98 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own outputs stored
+in tests/golden/ and against the CPU oracle on seeded workloads.
+
+Bars (from the backend's contract): U1 bit-exact; P within 1e-12 relative error with an
+absolute floor of 1e-300; identical error messages; group means within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+P_RTOL = 1e-12
+P_FLOOR = 1e-300
+
+
+def assert_p_close(P, Pref):
+    P, Pref = np.asarray(P), np.asarray(Pref)
+    err = np.abs(P - Pref) / np.maximum(np.abs(Pref), P_FLOOR)
+    bad = np.abs(P - Pref) > np.maximum(P_RTOL * np.abs(Pref), P_FLOOR)
+    assert not bad.any(), f"max rel err {err.max():.3e} at {np.argmax(err)}"
+
+
+def gene_major_to_target_major(flat, n_genes, n_targets):
+    return np.asarray(flat).reshape(n_genes, n_targets).T
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_cuda_matches_reference_fixture(name):
+    from hpdex_gb300.backend.bin import kernel
+    g = load_golden(name)
+    o = g["options"]
+    T, C = g["n_targets"], g["indptr"].size - 1
+    args = (g["data"], g["indices"], g["indptr"], g["group_id"], T)
+    kw = dict(tie_correction=o["tie_correction"], use_continuity=o["use_continuity"],
+              zero_handling=o["zero_handling"], alternative=o["alternative"], method=o["method"],
+              fast_norm=False)
+    if g["error"]:
+        with pytest.raises(RuntimeError) as e:
+            kernel.mannwhitneyu(*args, **kw)
+        assert str(e.value) == g["error"]
+    else:
+        U1, P = kernel.mannwhitneyu(*args, **kw)
+        assert U1.shape == (T, C)
+        np.testing.assert_array_equal(U1, gene_major_to_target_major(g["U1"], C, T))
+        assert_p_close(P, gene_major_to_target_major(g["P"], C, T))
+    G = T + 1
+    for include_zeros, key in ((True, "mean_kahan"), (False, "mean_kahan_nz")):
+        m = kernel.group_mean(g["data"], g["indices"], g["indptr"], g["group_id"], G,
+                              include_zeros=include_zeros)
+        ref = g[key]
+        np.testing.assert_allclose(m, ref, rtol=1e-6, atol=1e-12)
+
+
+def _oracle_compare(w, **opt):
+    from oracle import oracle
+    from hpdex_gb300.backend.bin import kernel
+    zh = {"none": 0, "min": 1, "max": 2, "mix": 3}[opt.get("zero_handling", "min")]
+    kw = dict(tie_correction=opt.get("tie_correction", True),
+              use_continuity=opt.get("use_continuity", True), zero_handling=zh,
+              alternative=opt.get("alternative", 2), method=opt.get("method", 2))
+    U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw)
+    U1o, Po = oracle.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw,
+                                  threads=-1)
+    C, T = w.n_cols, w.n_targets
+    np.testing.assert_array_equal(U1, gene_major_to_target_major(U1o, C, T))
+    assert_p_close(P, gene_major_to_target_major(Po, C, T))
+
+
+@pytest.mark.parametrize("zh", ["min", "max", "mix", "none"])
+def test_perturb_screen_reduced_matches_oracle(zh):
+    from hpdex_gb300 import synthetic
+    w = synthetic.perturb_screen(seed=21, n_rows=20_000, n_cols=300, n_targets=60, ref_size=2_000)
+    _oracle_compare(w, zero_handling=zh)
+
+
+def test_umi_counts_reduced_matches_oracle():
+    from hpdex_gb300 import synthetic
+    w = synthetic.umi_counts(seed=4, n_rows=10_000, n_cols=200, n_targets=15)
+    _oracle_compare(w, zero_handling="min")
+
+
+def test_batched_and_plain_forms_agree_and_repeat():
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix, BATCHED, PLAIN
+    w = synthetic.perturb_screen(seed=5, n_rows=8_000, n_cols=120, n_targets=25, ref_size=900)
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+    plan.run(BATCHED)
+    U1a, Pa = plan.download()
+    plan.run(BATCHED)  # graph replay
+    U1b, Pb = plan.download()
+    plan.run(PLAIN)
+    U1c, Pc = plan.download()
+    for U, P in ((U1b, Pb), (U1c, Pc)):
+        np.testing.assert_array_equal(U, U1a)
+        np.testing.assert_array_equal(P, Pa)
