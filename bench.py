@@ -1,0 +1,300 @@
+"""Benchmark of the MWU differential-expression path on one GB300.
+
+Workload (default): perturbation-screen scale, 200,000 cells x 8,000 genes, log1p-CP10k
+float32 (~1.47e8 nonzeros), 20,000 reference cells, 500 targets, zero_handling="min",
+tie and continuity corrections, two-sided asymptotic p-values. Synthetic, seeded.
+
+One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
+  value : tests/s with the matrix resident in HBM (library layout: float32 values, int32 row
+          ids, int64 column pointers, per-column key ranges), batched form (persistent
+          work-queue kernel + p-value kernel, replayed as one CUDA graph), device time from
+          CUDA events recorded inside the graph on the launching stream.
+  e2e   : tests/s through the reference-shaped public call kernel.mannwhitneyu with host
+          numpy arrays in and out (H2D of values, int64 row ids, column pointers and
+          group ids; D2H of U1 and P), wall clock.
+  plain : the same call in the plain form (one launch per gene, no graph, no queue).
+The inputs (1.17 GB resident) exceed the 129 MB L2, so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference backend (oracle/, OpenMP over all
+host cores) on a bounded sample of genes of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "gene x target MWU tests/s"
+UNIT = "tests/s"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per rank-kernel launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "mwu_rank_kernel_perturb_screen.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch_full_workload:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def make_workload(args, rank):
+    from hpdex_gb300 import synthetic
+    return synthetic.perturb_screen(seed=7 + rank)
+
+
+def algorithmic_bytes(w):
+    """Compulsory DRAM bytes of one rank-kernel launch: float32 value + int32 row id per
+    nonzero, the column pointers, the group ids, and U1 + tie sum (8 B each) per test."""
+    C, T = w.n_cols, w.n_targets
+    return w.nnz * 8 + 8 * (C + 1) + 4 * w.n_rows + 16 * C * T
+
+
+def cpu_sample(w, max_genes):
+    """Every k-th gene, so the sample keeps the gene-size distribution."""
+    k = max(1, w.n_cols // max_genes)
+    sel = np.arange(0, w.n_cols, k)
+    sizes = np.diff(w.indptr)[sel]
+    ip = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    idx = np.concatenate([np.arange(w.indptr[c], w.indptr[c + 1]) for c in sel])
+    return sel, w.data[idx], w.indices[idx], ip
+
+
+def time_cpu(w, max_genes, reps=1):
+    from oracle import oracle
+    sel, data, ind, ip = cpu_sample(w, max_genes)
+    best = None
+    for _ in range(reps):
+        t = time.perf_counter()
+        oracle.mannwhitneyu(data, ind, ip, w.group_id, w.n_targets, tie_correction=True,
+                            use_continuity=True, zero_handling=1, alternative=2, method=2,
+                            threads=-1)
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    tests = sel.size * w.n_targets
+    return tests / best, oracle.max_threads(), f"{sel.size} of {w.n_cols} genes (every {w.n_cols // sel.size}th), all 500 targets, {tests} tests, best of {reps}"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    w = make_workload(args, 0)
+    for _ in range(args.warmup):
+        time_cpu(w, 100)
+    vals = []
+    cores = None
+    sample = None
+    for _ in range(args.steps):
+        v, cores, sample = time_cpu(w, args.cpu_genes)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "perturb_screen 200000 cells x 8000 genes x 500 targets, "
+                               "log1p-CP10k float32, zero_handling=min", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world):
+    from hpdex_gb300 import _lib
+    from hpdex_gb300.backend.bin import kernel
+    from hpdex_gb300.resident import BATCHED, PLAIN, ResidentMatrix
+
+    if _lib.device_count() < 1:
+        raise RuntimeError("no CUDA device")
+    w = make_workload(args, rank)
+    T, C = w.n_targets, w.n_cols
+    tests = T * C
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
+    for _ in range(max(3, args.warmup)):
+        plan.run(BATCHED)
+    U1, P = plan.download()
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # host-side barrier / max only
+        dist.init_process_group("gloo")
+        dist.barrier()
+    sampler = ClockSampler(0)
+    t0 = time.perf_counter()
+    dev_ms, rank_ms, p_ms, launches = [], [], [], 0
+    for _ in range(args.steps):
+        plan.run(BATCHED)  # synchronous: graph replay + sync + error check
+        (tot, rk, pv), nl = plan.timings()
+        dev_ms.append(tot)
+        rank_ms.append(rk)
+        p_ms.append(pv)
+        launches += nl
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    elapsed_dev = sum(dev_ms) / 1e3
+    if dist is not None:
+        import torch
+        t = torch.tensor([elapsed_dev, wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_dev, wall = float(t[0]), float(t[1])
+    value = world * tests * args.steps / elapsed_dev
+
+    # plain form (one launch per gene, no graph, no queue), one step
+    t1 = time.perf_counter()
+    plan.run(PLAIN)
+    (ptot, prk, ppv), pl = plan.timings()
+    plain_wall = time.perf_counter() - t1
+    U1p, Pp = plan.download()
+    same = bool(np.array_equal(U1p, U1) and np.array_equal(Pp, P))
+
+    # end to end through the public call: host arrays in, host arrays out
+    h2d = w.nnz * (w.data.itemsize + 8) + 8 * (C + 1) + 4 * w.n_rows
+    d2h = 2 * 8 * tests
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T, tie_correction=True,
+                        use_continuity=True, zero_handling=1)  # warm (allocations, module load)
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        U1e, Pe = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T,
+                                      tie_correction=True, use_continuity=True, zero_handling=1)
+    e2e_wall = (time.perf_counter() - te) / e2e_steps
+    same = same and bool(np.array_equal(U1e, U1) and np.array_equal(Pe, P))
+
+    hbm, peak_kind = peaks()
+    B = algorithmic_bytes(w)
+    rank_avg = statistics.mean(rank_ms) / 1e3
+    achieved = B / rank_avg / 1e9
+    traffic = traffic_from_profile()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(dev_ms),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 keys / i64 rank sums / f64 p", "data": "synthetic",
+        "config": {"workload": "perturb_screen: 200000 cells x 8000 genes, log1p-CP10k float32, "
+                               f"nnz={w.nnz}, 20000 reference cells, {T} targets, "
+                               "zero_handling=min, tie+continuity, two-sided asymptotic",
+                   "form": "batched (persistent work-queue kernel + CUDA graph)",
+                   "l2": "inputs 1.17 GB resident > 129 MB L2 (no flush needed)",
+                   "wall_ms_per_step": wall / args.steps * 1e3},
+        "e2e": {"value": world * tests / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_wall * 1e3,
+                "call": "hpdex_gb300.backend.bin.kernel.mannwhitneyu (host numpy in/out)"},
+        "plain": {"value": tests / (ptot / 1e3), "unit": UNIT, "ms_per_step": ptot,
+                  "wall_ms": plain_wall * 1e3, "launches": pl,
+                  "batched_speedup": (tests / elapsed_dev * args.steps) / (tests / (ptot / 1e3)),
+                  "results_identical": same},
+        "kernels_ms": {"rank": statistics.mean(rank_ms), "pvalue": statistics.mean(p_ms)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "kernel": "mwu_rank_kernel", "algorithmic_bytes": B,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        cpu_v, cores, sample = time_cpu(w, args.cpu_genes)
+        line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": sample}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-genes", type=int, default=800)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        # one process per GPU: each rank sees only its own device (independent replicas)
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

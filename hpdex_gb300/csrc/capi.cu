@@ -54,7 +54,7 @@ int fail(int code, const char* fmt, ...) {
         if (_s != HPDEX_OK) return _s;   \
     } while (0)
 
-constexpr int kRankThreads = 512;
+constexpr int kRankThreads = 1024;
 constexpr int kMeanThreads = 256;
 
 struct DeviceInfo {
@@ -130,6 +130,8 @@ struct hpdex_matrix {
     DevBuf<unsigned char> data;
     DevBuf<int32_t> rows;
     DevBuf<int64_t> indptr;
+    DevBuf<unsigned long long> col_kmin, col_kmax;  // per-column key range (resident layout)
+    DevBuf<unsigned char> col_has_zero;
     std::vector<long long> col_nnz;  // host copy for scheduling
     long long max_col_nnz = 0;
     DeviceInfo dev;
@@ -148,10 +150,10 @@ struct hpdex_plan {
     DevBuf<double> U1, P;
     DevBuf<uint32_t> n1, n2;  // zero_handling = none
     // rank scratch
-    DevBuf<unsigned char> ek, tk;
-    DevBuf<uint32_t> eg, tg;
+    DevBuf<unsigned char> ek;
+    DevBuf<uint32_t> eg;
     DevBuf<unsigned char> acc;
-    DevBuf<uint32_t> tiecnt;
+    DevBuf<uint32_t> cnt;
     RankArgs ra{};
     size_t rank_smem = 0;
     int rank_grid = 0;
@@ -210,8 +212,25 @@ template <class V>
 struct RankOccupancy {
     static int run(size_t smem, size_t smem_max, int* blocks) {
         auto k = mwu_rank_kernel<V, kRankThreads>;
-        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+        cudaFuncAttributes fa;
+        CUDA_TRY(cudaFuncGetAttributes(&fa, k));
+        // the opt-in limit covers static + dynamic shared memory
+        const int max_dyn = (int)(smem_max - fa.sharedSizeBytes);
+        if ((size_t)max_dyn < smem) return fail(HPDEX_ERR_CUDA, "rank kernel shared memory %zu exceeds %d", smem, max_dyn);
+        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn));
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, kRankThreads, smem));
+        return HPDEX_OK;
+    }
+};
+template <class V>
+struct KeyRangeLaunch {
+    static int run(hpdex_matrix* m) {
+        const int threads = 256, wpb = threads / 32;
+        const int grid = (int)std::max<long long>(1, std::min<long long>((m->n_cols + wpb - 1) / wpb, 65535));
+        column_key_range_kernel<V><<<grid, threads>>>(reinterpret_cast<const V*>(m->data.p), m->indptr.p,
+                                                     (int32_t)m->n_cols, m->col_kmin.p, m->col_kmax.p,
+                                                     m->col_has_zero.p);
+        CUDA_TRY(cudaGetLastError());
         return HPDEX_OK;
     }
 };
@@ -260,6 +279,14 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
         }
         CUDA_TRY(cudaDeviceSynchronize());
     }
+    // per-column key range of finite nonzero values: the bucket function of every plan
+    TRY(m->col_kmin.alloc(std::max<long long>(m->n_cols, 1)));
+    TRY(m->col_kmax.alloc(std::max<long long>(m->n_cols, 1)));
+    TRY(m->col_has_zero.alloc(std::max<long long>(m->n_cols, 1)));
+    if (m->n_cols) {
+        TRY(dispatch_dtype<KeyRangeLaunch>(m->dtype, m));
+        CUDA_TRY(cudaDeviceSynchronize());
+    }
     m->col_nnz.resize((size_t)m->n_cols);
     m->max_col_nnz = 0;
     for (long long c = 0; c < m->n_cols; ++c) {
@@ -269,27 +296,25 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
     return HPDEX_OK;
 }
 
-// Rank-kernel layout for this plan: 2 CTAs per SM when the layout fits, else 1.
+// Rank-kernel layout for this plan: one 1024-thread CTA per SM; the bucket table takes
+// 2^13 entries, then the per-target accumulators, the run counters of as many warps as fit
+// (at least 4, else in global memory), and the rest holds a gene's elements when it fits.
 int configure_rank(hpdex_plan* p) {
     const hpdex_matrix* m = p->m;
     const int kb = key_bytes(m->dtype);
     const int G = (int)p->G;
-    const int tie_warps = 4;
-    const int nbl = 12;
-    size_t budget = 0;
-    int per_sm = 2;
-    for (; per_sm >= 1; --per_sm) {
-        budget = m->dev.smem_per_sm / per_sm - m->dev.smem_reserved - 1024;
-        budget = std::min(budget, m->dev.smem_optin);
-        const RankSmem base(nbl, G, tie_warps, 0, 0, 0, kb);
-        if (base.total + 4096 <= budget) break;
-    }
-    if (per_sm < 1) per_sm = 1;
-    int acc_in = 1, cnt_in = 1;
+    const int nbl = 13;
+    const size_t budget = std::min(m->dev.smem_per_sm - m->dev.smem_reserved, m->dev.smem_optin) - 2048;
+    int acc_in = 1, cnt_in = 1, tie_warps = kRankThreads / 32;
     RankSmem L(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
-    if (L.total > budget) { cnt_in = 0; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
+    while (L.total > budget && tie_warps > 4) {
+        tie_warps /= 2;
+        L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
+    }
+    if (L.total > budget) { cnt_in = 0; tie_warps = kRankThreads / 32; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
     if (L.total > budget) { acc_in = 0; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
-    const size_t left = budget > L.total ? budget - L.total : 0;
+    if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
+    const size_t left = budget - L.total;
     int cap = (int)std::min<size_t>(left / (kb + 4), (size_t)1 << 30);
     cap = std::max(0, cap - 8);
     L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
@@ -306,15 +331,16 @@ int configure_rank(hpdex_plan* p) {
         TRY(p->ek.alloc(nctas * slice * kb));
         TRY(p->eg.alloc(nctas * slice));
     }
-    TRY(p->tk.alloc(nctas * slice * kb));
-    TRY(p->tg.alloc(nctas * slice));
     if (!acc_in) TRY(p->acc.alloc(nctas * 24 * (size_t)G));
-    if (!cnt_in) TRY(p->tiecnt.alloc(nctas * tie_warps * (size_t)G));
+    if (!cnt_in) TRY(p->cnt.alloc(nctas * tie_warps * (size_t)RankSmem::cnt_words(G)));
 
     RankArgs& a = p->ra;
     a.data = m->data.p;
     a.rows = m->rows.p;
     a.indptr = m->indptr.p;
+    a.col_kmin = m->col_kmin.p;
+    a.col_kmax = m->col_kmax.p;
+    a.col_has_zero = m->col_has_zero.p;
     a.n_rows = m->n_rows;
     a.n_cols = (int32_t)m->n_cols;
     a.G = G;
@@ -332,15 +358,13 @@ int configure_rank(hpdex_plan* p) {
     a.err = p->err.p;
     a.ek_global = p->ek.p;
     a.eg_global = p->eg.p;
-    a.tk_global = p->tk.p;
-    a.tg_global = p->tg.p;
     a.slice = slice;
     a.acc_global = p->acc.p;
-    a.tiecnt_global = p->tiecnt.p;
+    a.cnt_global = p->cnt.p;
     a.nb_max_log2 = nbl;
     a.elem_smem_cap = cap;
     a.acc_in_smem = acc_in;
-    a.tiecnt_in_smem = cnt_in;
+    a.cnt_in_smem = cnt_in;
     a.tie_warps = tie_warps;
     return HPDEX_OK;
 }
@@ -642,13 +666,15 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
             CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int st = HPDEX_OK;
             int l = 0;
-            if (cudaEventRecord(p->ev[0], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            // event-record nodes (a plain record under capture only adds a dependency)
+            const unsigned ext = cudaEventRecordExternal;
+            if (cudaEventRecordWithFlags(p->ev[0], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
             if (st == HPDEX_OK && cudaMemsetAsync(p->err.p, 0xff, 2 * sizeof(unsigned long long), s) != cudaSuccess)
                 st = fail(HPDEX_ERR_CUDA, "memset failed");
             if (st == HPDEX_OK) st = enqueue_rank(p, mode, s, &l);
-            if (st == HPDEX_OK && cudaEventRecord(p->ev[1], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            if (st == HPDEX_OK && cudaEventRecordWithFlags(p->ev[1], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
             if (st == HPDEX_OK) st = launch_pvalues_asymptotic(p, s);
-            if (st == HPDEX_OK && cudaEventRecord(p->ev[2], s) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
+            if (st == HPDEX_OK && cudaEventRecordWithFlags(p->ev[2], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (st != HPDEX_OK) { if (g) cudaGraphDestroy(g); return st; }
@@ -674,9 +700,9 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
     }
     CUDA_TRY(cudaStreamSynchronize(s));
     p->last_launches = launches;
-    cudaEventElapsedTime(&p->last_ms[0], p->ev[0], p->ev[2]);
-    cudaEventElapsedTime(&p->last_ms[1], p->ev[0], p->ev[1]);
-    cudaEventElapsedTime(&p->last_ms[2], p->ev[1], p->ev[2]);
+    CUDA_TRY(cudaEventElapsedTime(&p->last_ms[0], p->ev[0], p->ev[2]));
+    CUDA_TRY(cudaEventElapsedTime(&p->last_ms[1], p->ev[0], p->ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(&p->last_ms[2], p->ev[1], p->ev[2]));
     return check_device_errors(p);
 }
 

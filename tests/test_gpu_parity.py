@@ -60,19 +60,36 @@ def _oracle_compare(w, **opt):
     kw = dict(tie_correction=opt.get("tie_correction", True),
               use_continuity=opt.get("use_continuity", True), zero_handling=zh,
               alternative=opt.get("alternative", 2), method=opt.get("method", 2))
+    try:
+        U1o, Po = oracle.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                      **kw, threads=-1)
+    except RuntimeError as e:  # the reference raises: the GPU path must raise the same text
+        with pytest.raises(RuntimeError) as e2:
+            kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw)
+        assert str(e2.value) == str(e)
+        return "error"
     U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw)
-    U1o, Po = oracle.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw,
-                                  threads=-1)
     C, T = w.n_cols, w.n_targets
     np.testing.assert_array_equal(U1, gene_major_to_target_major(U1o, C, T))
     assert_p_close(P, gene_major_to_target_major(Po, C, T))
+    return "ok"
 
 
 @pytest.mark.parametrize("zh", ["min", "max", "mix", "none"])
 def test_perturb_screen_reduced_matches_oracle(zh):
     from hpdex_gb300 import synthetic
     w = synthetic.perturb_screen(seed=21, n_rows=20_000, n_cols=300, n_targets=60, ref_size=2_000)
-    _oracle_compare(w, zero_handling=zh)
+    # 'none' ranks explicit values only, so sparse genes make targets too small: both raise
+    assert _oracle_compare(w, zero_handling=zh) == ("error" if zh == "none" else "ok")
+
+
+@pytest.mark.parametrize("alt", [0, 1, 2])
+def test_dense_signed_none_mode_matches_oracle(alt):
+    """zero_handling='none' on dense signed data with shifted targets and ties."""
+    from hpdex_gb300 import synthetic
+    w = synthetic.exact_small(seed=8, n_rows=3_000, n_cols=64, n_targets=40, ref_size=200)
+    w.data = np.round(w.data * 8) / 8  # many ties, explicit zeros stay explicit in 'none'
+    assert _oracle_compare(w, zero_handling="none", alternative=alt, use_continuity=False) == "ok"
 
 
 def test_umi_counts_reduced_matches_oracle():
