@@ -64,6 +64,11 @@ EXPORTS = {
     "hpdex_plan_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                           ctypes.POINTER(ctypes.c_int32)]),
+    "hpdex_mannwhitneyu_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                                  ctypes.c_void_p, ctypes.c_int64,
+                                                  ctypes.POINTER(MwuOptions), ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

@@ -796,3 +796,271 @@ int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
 }
 
 }  // extern "C"
+
+// =======================================================================================
+// No-allocation entry point.
+//
+// For callers that must not allocate device memory during a call: code that runs inside a
+// framework's own memory pool or caching allocator (where a cudaMalloc/cudaFree would
+// bypass the pool and can synchronise the device), latency-critical serving paths that
+// reserve all memory up front, and hosts embedding this library behind a plugin interface
+// that forbids allocation. The caller passes device buffers for every input and output;
+// the rest of the working memory is one file-scope device array of fixed size,
+// kNoAllocScratchBytes, which every GPU that loads this library holds until process exit.
+// =======================================================================================
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = HPDEX_NOALLOC_SCRATCH_BYTES;  // 64 MiB per device
+constexpr int kNoAllocMaxGroups = HPDEX_NOALLOC_MAX_GROUPS;           // n_targets + 1
+constexpr long long kNoAllocMaxCols = HPDEX_NOALLOC_MAX_COLS;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+    unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+    DeviceInfo info;
+};
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[64];
+
+// Set-up, once per device, with that device current: the host-side symbol is only a
+// stand-in, kernels must get the device address.
+int noalloc_setup(int dev, NoAllocDevice** out) {
+    if (dev < 0 || dev >= 64) return fail(HPDEX_ERR_UNSUPPORTED, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.scratch) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(HPDEX_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch) failed: %s",
+                        cudaGetErrorString(e));
+        TRY(device_info(d.info));
+        d.scratch = static_cast<unsigned char*>(ptr);
+    }
+    *out = &d;
+    return HPDEX_OK;
+}
+
+// group sizes (reference group_rows, mannwhitneyu.cpp:865-869), the longest column, and
+// the identity gene order for the work queue
+__global__ void noalloc_prepare_kernel(const int32_t* gid, long long n_rows, int G,
+                                       const int64_t* indptr, int n_cols, long long* group_rows,
+                                       unsigned long long* max_col, int32_t* order) {
+    __shared__ unsigned int cnt[kNoAllocMaxGroups];
+    for (int g = threadIdx.x; g < G; g += blockDim.x) cnt[g] = 0u;
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += stride) {
+        const int g = gid[r];
+        if (g >= 0 && g < G) atomicAdd(&cnt[g], 1u);
+    }
+    unsigned long long mx = 0;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += stride) {
+        const unsigned long long len = (unsigned long long)(indptr[c + 1] - indptr[c]);
+        mx = len > mx ? len : mx;
+        order[c] = (int32_t)c;
+    }
+    __syncthreads();
+    for (int g = threadIdx.x; g < G; g += blockDim.x)
+        if (cnt[g]) atomicAdd(reinterpret_cast<unsigned long long*>(&group_rows[g]), (unsigned long long)cnt[g]);
+    mx = warp_max(mx);
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_col, mx);
+}
+
+template <class V>
+struct NoAllocKeyRange {
+    static int run(const void* data, const int64_t* indptr, int32_t n_cols, unsigned long long* kmin,
+                   unsigned long long* kmax, unsigned char* hz, cudaStream_t s) {
+        const int threads = 256, wpb = threads / 32;
+        const int grid = (int)std::max<long long>(1, std::min<long long>((n_cols + wpb - 1) / wpb, 65535));
+        column_key_range_kernel<V><<<grid, threads, 0, s>>>(reinterpret_cast<const V*>(data), indptr,
+                                                           n_cols, kmin, kmax, hz);
+        CUDA_TRY(cudaGetLastError());
+        return HPDEX_OK;
+    }
+};
+template <class V>
+struct NoAllocRank {
+    static int run(const RankArgs* a, int grid, size_t smem, cudaStream_t s) {
+        auto k = mwu_rank_kernel<V, kRankThreads>;
+        k<<<grid, kRankThreads, smem, s>>>(*a);
+        CUDA_TRY(cudaGetLastError());
+        return HPDEX_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, const int32_t* d_rows,
+                                          const int64_t* d_indptr, int64_t n_rows, int64_t n_cols,
+                                          const int32_t* d_group_id, int64_t n_targets,
+                                          const hpdex_mwu_options* opt, double* d_U1,
+                                          double* d_P, void* stream) {
+    if (!opt) return fail(HPDEX_ERR_ARGUMENT, "options are NULL");
+    if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    if (dtype_size(dtype) == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
+    if (opt->method != HPDEX_ASYMPTOTIC)
+        return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc supports method=asymptotic only");
+    if (opt->zero_handling < 0 || opt->zero_handling > 3) return fail(HPDEX_ERR_ARGUMENT, "zero_handling must be 0..3");
+    if (opt->alternative < 0 || opt->alternative > 2) return fail(HPDEX_ERR_ARGUMENT, "alternative must be 0..2");
+    if (n_targets + 1 > kNoAllocMaxGroups)
+        return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: n_targets + 1 = %lld exceeds %d",
+                    (long long)(n_targets + 1), kNoAllocMaxGroups);
+    if (n_cols < 0 || n_cols > kNoAllocMaxCols)
+        return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: n_cols = %lld outside [0, %lld]",
+                    (long long)n_cols, kNoAllocMaxCols);
+    if (n_rows < 0 || n_rows >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "n_rows must be in [0, 2^31)");
+    if (!d_indptr || (n_rows > 0 && !d_group_id) || (n_cols > 0 && n_targets > 0 && (!d_U1 || !d_P)))
+        return fail(HPDEX_ERR_ARGUMENT, "NULL device pointer");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    NoAllocDevice* nd = nullptr;
+    TRY(noalloc_setup(dev, &nd));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int G = (int)(n_targets + 1);
+    const long long C = n_cols, T = n_targets;
+    const int zh = opt->zero_handling;
+    const int kb = key_bytes(dtype);
+
+    // carve the scratch: header | group_rows | per-column arrays | none-mode sizes | elements
+    unsigned char* base = nd->scratch;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { unsigned char* p = base + off; off = RankSmem::align16(off + bytes); return p; };
+    int32_t* queue = reinterpret_cast<int32_t*>(take(sizeof(int32_t)));
+    unsigned long long* err = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
+    unsigned long long* max_col = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+    long long* group_rows = reinterpret_cast<long long*>(take(sizeof(long long) * G));
+    const size_t header_bytes = off;
+    int32_t* order = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * std::max<long long>(C, 1)));
+    unsigned long long* kmin = reinterpret_cast<unsigned long long*>(take(8 * std::max<long long>(C, 1)));
+    unsigned long long* kmax = reinterpret_cast<unsigned long long*>(take(8 * std::max<long long>(C, 1)));
+    unsigned char* has_zero = take(std::max<long long>(C, 1));
+    uint32_t* n1 = nullptr;
+    uint32_t* n2 = nullptr;
+    if (zh == HPDEX_ZERO_NONE) {
+        const size_t need = sizeof(uint32_t) * (size_t)(C + T * C);
+        if (off + need > kNoAllocScratchBytes)
+            return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: zero_handling=none needs %zu scratch bytes for sample sizes", need);
+        n1 = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * std::max<long long>(C, 1)));
+        n2 = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * std::max<long long>(T * C, 1)));
+    }
+
+    // every call shares the array and finds the previous call's contents: clear what
+    // must start at zero (work counter, group sizes, longest column) and reset the error words
+    CUDA_TRY(cudaMemsetAsync(base, 0, header_bytes, s));
+    CUDA_TRY(cudaMemsetAsync(err, 0xff, 2 * sizeof(unsigned long long), s));
+    if (C == 0) return HPDEX_OK;
+    {
+        const int grid = (int)std::min<long long>(std::max<long long>((std::max<long long>((long long)n_rows, C) + 255) / 256, 1),
+                                                  (long long)nd->info.sms * 4);
+        noalloc_prepare_kernel<<<grid, 256, 0, s>>>(d_group_id, n_rows, G, d_indptr, (int)C, group_rows,
+                                                    max_col, order);
+        CUDA_TRY(cudaGetLastError());
+    }
+    long long rows_host[kNoAllocMaxGroups];
+    unsigned long long longest = 0;
+    CUDA_TRY(cudaMemcpyAsync(rows_host, group_rows, sizeof(long long) * G, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&longest, max_col, sizeof(longest), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    if (zh != HPDEX_ZERO_NONE) {  // same checks and messages as hpdex_plan_create
+        if (rows_host[0] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column 0");
+        for (int g = 1; g < G; ++g)
+            if (rows_host[g] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %d at column 0", g);
+    }
+
+    // rank-kernel layout (same sizing rule as the plan path); accumulators and run counters
+    // must fit in shared memory here, which kNoAllocMaxGroups guarantees
+    const int nbl = 13;
+    const size_t budget = std::min(nd->info.smem_per_sm - nd->info.smem_reserved, nd->info.smem_optin) - 2048;
+    int tie_warps = kRankThreads / 32;
+    RankSmem L(nbl, G, tie_warps, 1, 1, 0, kb);
+    while (L.total > budget && tie_warps > 4) {
+        tie_warps /= 2;
+        L = RankSmem(nbl, G, tie_warps, 1, 1, 0, kb);
+    }
+    if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: layout does not fit");
+    int cap = (int)std::min<size_t>((budget - L.total) / (kb + 4), (size_t)1 << 30);
+    cap = std::max(0, cap - 8);
+    L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
+    int blocks = 0;
+    TRY(dispatch_dtype<RankOccupancy>(dtype, L.total, nd->info.smem_optin, &blocks));
+    if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM");
+    const int grid = nd->info.sms * blocks;
+    long long slice = 0;
+    if ((long long)longest > cap) {
+        const size_t left = off < kNoAllocScratchBytes ? kNoAllocScratchBytes - off - 256 * (size_t)grid : 0;
+        slice = (long long)(left / ((size_t)grid * (kb + 4)));
+        if ((long long)longest > slice)
+            return fail(HPDEX_ERR_UNSUPPORTED,
+                        "hpdex_mannwhitneyu_noalloc: a column holds %llu entries, above the %lld the "
+                        "fixed scratch allows at this size", longest, slice);
+    }
+    void* ek = slice ? take((size_t)grid * slice * kb) : nullptr;
+    uint32_t* eg = slice ? reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4)) : nullptr;
+
+    TRY(dispatch_dtype<NoAllocKeyRange>(dtype, d_data, d_indptr, (int32_t)C, kmin, kmax, has_zero, s));
+    RankArgs a{};
+    a.data = d_data;
+    a.rows = d_rows;
+    a.indptr = d_indptr;
+    a.col_kmin = kmin;
+    a.col_kmax = kmax;
+    a.col_has_zero = has_zero;
+    a.n_rows = n_rows;
+    a.n_cols = (int32_t)C;
+    a.G = G;
+    a.gid = d_group_id;
+    a.order = order;
+    a.queue = queue;
+    a.single_gene = -1;
+    a.zero_handling = zh;
+    a.tie_correction = opt->tie_correction;
+    a.group_rows = group_rows;
+    a.U1 = d_U1;
+    a.tie = d_P;
+    a.n1 = n1;
+    a.n2 = n2;
+    a.err = err;
+    a.ek_global = ek;
+    a.eg_global = eg;
+    a.slice = std::max<long long>(slice, 1);
+    a.acc_global = nullptr;
+    a.cnt_global = nullptr;
+    a.nb_max_log2 = nbl;
+    a.elem_smem_cap = cap;
+    a.acc_in_smem = 1;
+    a.cnt_in_smem = 1;
+    a.tie_warps = tie_warps;
+    TRY(dispatch_dtype<NoAllocRank>(dtype, &a, grid, L.total, s));
+
+    PArgs pa{};
+    pa.U1 = d_U1;
+    pa.P = d_P;
+    pa.n = T * C;
+    pa.n_cols = (int32_t)C;
+    pa.group_rows = group_rows;
+    pa.n1g = n1;
+    pa.n2t = n2;
+    pa.zero_handling = zh;
+    pa.alternative = opt->alternative;
+    pa.cc = opt->use_continuity ? 0.5 : 0.0;
+    mwu_pvalue_asymptotic_kernel<<<(int)std::min<long long>((pa.n + 255) / 256, (long long)nd->info.sms * 8), 256, 0, s>>>(pa);
+    CUDA_TRY(cudaGetLastError());
+
+    unsigned long long e[2];
+    CUDA_TRY(cudaMemcpyAsync(e, err, sizeof e, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    const unsigned long long Gu = (unsigned long long)G;
+    if (e[0] != ~0ull) {
+        const unsigned long long c = e[0] / Gu, g = e[0] % Gu;
+        if (g == 0) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column %llu", c);
+        return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %llu at column %llu", g, c);
+    }
+    if (e[1] != ~0ull) {
+        const unsigned long long c = e[1] / Gu, g = e[1] % Gu;
+        return fail(HPDEX_ERR_ARGUMENT, "column %llu stores more entries for group %llu than the group has rows "
+                    "(duplicate row indices)", c, g);
+    }
+    return HPDEX_OK;
+}

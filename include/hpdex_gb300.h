@@ -141,6 +141,44 @@ int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
  * launches it made. */
 int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches);
 
+/* ---- no-allocation variant (no counterpart in the reference) ----
+ *
+ * hpdex_mannwhitneyu_noalloc computes the same U1 / P as hpdex_mannwhitneyu but allocates
+ * nothing: no cudaMalloc, no cudaFree, no allocating library routine. It is meant for
+ * callers that cannot allocate device memory during a call -- code running inside a
+ * framework's own memory pool or caching allocator (a raw cudaMalloc/cudaFree would bypass
+ * the pool and can synchronise the device), serving loops that reserve all memory up front
+ * for predictable latency, and plugin hosts that forbid allocation.
+ *
+ * The caller passes device pointers: d_data (the values in CSC order, d_indptr[n_cols] of
+ * them), d_rows (int32 row ids, the library's resident layout), d_indptr (int64,
+ * n_cols + 1), d_group_id (int32, n_rows) and the outputs d_U1 / d_P (n_targets * n_cols
+ * doubles, target-major). `stream` is a cudaStream_t (NULL = legacy default stream). The call
+ * synchronises that stream before returning.
+ *
+ * Working memory is one fixed device array of HPDEX_NOALLOC_SCRATCH_BYTES inside the
+ * library; every GPU that loads the library holds it until the process exits. Limits:
+ * n_targets + 1 <= HPDEX_NOALLOC_MAX_GROUPS, n_cols <= HPDEX_NOALLOC_MAX_COLS,
+ * method = HPDEX_ASYMPTOTIC only, and the longest column must fit the per-SM element
+ * slices that remain in the array (about 50k entries for float32 data); anything beyond
+ * returns HPDEX_ERR_UNSUPPORTED with a message. Genes are taken in column order (no
+ * longest-first scheduling).
+ *
+ * The first call on a device does a one-time set-up (it resolves the device address of
+ * the array with cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the one array and finds the previous call's contents in it: calls
+ * that overlap on the GPU (two host threads, or two streams) race and corrupt each other,
+ * so serialise them.
+ */
+#define HPDEX_NOALLOC_SCRATCH_BYTES (64u << 20)
+#define HPDEX_NOALLOC_MAX_GROUPS 1024
+#define HPDEX_NOALLOC_MAX_COLS 262144
+int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, const int32_t* d_rows,
+                               const int64_t* d_indptr, int64_t n_rows, int64_t n_cols,
+                               const int32_t* d_group_id, int64_t n_targets,
+                               const hpdex_mwu_options* opt, double* d_U1, double* d_P,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif
