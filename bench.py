@@ -215,6 +215,16 @@ def run_ours(args, rank, world):
         elapsed_dev, wall = float(t[0]), float(t[1])
     value = world * tests * args.steps / elapsed_dev
 
+    line_core = {"value": value, "ms_per_step": statistics.mean(dev_ms),
+                 "rank_ms": statistics.mean(rank_ms), "pvalue_ms": statistics.mean(p_ms)}
+    if args.only_batched:  # profiling runs: the timed batched steps only
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "form": "batched", **line_core}),
+                  flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
     # plain form (one launch per gene, no graph, no queue), one step
     t1 = time.perf_counter()
     plan.run(PLAIN)
@@ -286,6 +296,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-genes", type=int, default=800)
+    ap.add_argument("--only-batched", action="store_true",
+                    help="time the batched form only (no plain form, e2e or CPU legs); for ncu")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:

@@ -1,8 +1,9 @@
 """Build recipe of the native library (nvcc, sm_103a only; no cmake, no torch).
 
-`build()` compiles hpdex_gb300/csrc/capi.cu (which includes every kernel header) into
-hpdex_gb300/lib/libhpdex_gb300.so. It runs in a few seconds and works without a GPU
-(nvcc cross-compiles), so the same call builds on the x86 host and on the Arm GPU host.
+`build()` compiles every hpdex_gb300/csrc/*.cu translation unit in parallel (the rank kernel
+has one unit per value type) and links them into hpdex_gb300/lib/libhpdex_gb300.so. It works
+without a GPU (nvcc cross-compiles), so the same call builds on the x86 host and on the Arm
+GPU host.
 """
 from __future__ import annotations
 
@@ -26,7 +27,7 @@ def nvcc() -> str:
 
 def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
-                  if f.endswith((".cu", ".cuh")))
+                  if f.endswith((".cu", ".cuh", ".h")))
 
 
 def up_to_date() -> bool:
@@ -41,11 +42,22 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)
+    objdir = os.path.join(LIBDIR, "obj")
+    os.makedirs(objdir, exist_ok=True)
+    units = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    procs = []
+    for u in units:
+        obj = os.path.join(objdir, u[:-3] + ".o")
+        cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
+               "-c", "-o", obj, os.path.join(CSRC, u)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        procs.append((u, subprocess.Popen(cmd)))
+    failed = [u for u, p in procs if p.wait() != 0]
+    if failed:
+        raise RuntimeError(f"nvcc failed for {failed}")
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
-           "-shared", "-o", tmp, os.path.join(CSRC, "capi.cu")]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+    objs = [os.path.join(objdir, u[:-3] + ".o") for u in units]
+    subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs], check=True)
     os.replace(tmp, LIB)
     return LIB

@@ -23,6 +23,7 @@
 #include "group_mean.cuh"
 #include "mwu_rank.cuh"
 #include "pvalue.cuh"
+#include "rank_launch.h"
 
 using namespace hpdex;
 
@@ -149,9 +150,9 @@ struct hpdex_plan {
     DevBuf<unsigned long long> err;
     DevBuf<double> U1, P;
     DevBuf<uint32_t> n1, n2;  // zero_handling = none
-    // rank scratch
-    DevBuf<unsigned char> ek;
-    DevBuf<uint32_t> eg;
+    // rank scratch: decoded column and bucket-ordered slab, one slice per CTA each
+    DevBuf<unsigned char> dk, ek;
+    DevBuf<uint32_t> dg, eg;
     DevBuf<unsigned char> acc;
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
@@ -197,31 +198,11 @@ int dispatch_dtype(int dt, Args&&... args) {
     }
 }
 
-template <class V>
-struct RankLaunch {
-    static int run(hpdex_plan* p, dim3 grid, cudaStream_t s) {
-        // the dynamic shared-memory limit was raised to the device maximum when the plan
-        // was configured (RankOccupancy), so no attribute call happens under capture
-        auto k = mwu_rank_kernel<V, kRankThreads>;
-        k<<<grid, kRankThreads, p->rank_smem, s>>>(p->ra);
-        CUDA_TRY(cudaGetLastError());
-        return HPDEX_OK;
-    }
-};
-template <class V>
-struct RankOccupancy {
-    static int run(size_t smem, size_t smem_max, int* blocks) {
-        auto k = mwu_rank_kernel<V, kRankThreads>;
-        cudaFuncAttributes fa;
-        CUDA_TRY(cudaFuncGetAttributes(&fa, k));
-        // the opt-in limit covers static + dynamic shared memory
-        const int max_dyn = (int)(smem_max - fa.sharedSizeBytes);
-        if ((size_t)max_dyn < smem) return fail(HPDEX_ERR_CUDA, "rank kernel shared memory %zu exceeds %d", smem, max_dyn);
-        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn));
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, kRankThreads, smem));
-        return HPDEX_OK;
-    }
-};
+int rank_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return HPDEX_OK;
+    return fail(HPDEX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
 template <class V>
 struct KeyRangeLaunch {
     static int run(hpdex_matrix* m) {
@@ -304,35 +285,35 @@ int configure_rank(hpdex_plan* p) {
     const int kb = key_bytes(m->dtype);
     const int G = (int)p->G;
     const int nbl = 13;
+    const int tie_warps = kRankThreads / 32;  // every warp resolves buckets
     const size_t budget = std::min(m->dev.smem_per_sm - m->dev.smem_reserved, m->dev.smem_optin) - 2048;
-    int acc_in = 1, cnt_in = 1, tie_warps = kRankThreads / 32;
+    // accumulators and run counters live together: both in shared memory, or both global
+    int acc_in = 1, cnt_in = 1;
     RankSmem L(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
-    while (L.total > budget && tie_warps > 4) {
-        tie_warps /= 2;
-        L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
-    }
-    if (L.total > budget) { cnt_in = 0; tie_warps = kRankThreads / 32; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
-    if (L.total > budget) { acc_in = 0; L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, 0, kb); }
+    if (L.total + 16384 > budget) { acc_in = cnt_in = 0; L = RankSmem(nbl, G, tie_warps, 0, 0, 0, kb); }
     if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
     const size_t left = budget - L.total;
-    int cap = (int)std::min<size_t>(left / (kb + 4), (size_t)1 << 30);
+    int cap = (int)std::min<size_t>(left / (kb + 5), (size_t)1 << 30);  // + big-list entry share
     cap = std::max(0, cap - 8);
     L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
     p->rank_smem = L.total;
 
     int blocks = 0;
-    TRY(dispatch_dtype<RankOccupancy>(m->dtype, p->rank_smem, m->dev.smem_optin, &blocks));
+    TRY(rank_status(rank_occupancy(m->dtype, p->rank_smem, m->dev.smem_optin, acc_in, &blocks), "rank kernel set-up"));
     if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM (smem %zu)", p->rank_smem);
     p->rank_grid = m->dev.sms * blocks;
 
-    const long long slice = std::max<long long>(1, m->max_col_nnz);
+    // multiple of 8 elements: every CTA's slice starts 32-byte aligned for vector access
+    const long long slice = (m->max_col_nnz + 8 + 7) & ~7ll;
     const size_t nctas = (size_t)p->rank_grid;
+    TRY(p->dk.alloc(nctas * slice * kb));
+    TRY(p->dg.alloc(nctas * slice));
     if ((long long)cap < m->max_col_nnz) {
         TRY(p->ek.alloc(nctas * slice * kb));
         TRY(p->eg.alloc(nctas * slice));
     }
     if (!acc_in) TRY(p->acc.alloc(nctas * 24 * (size_t)G));
-    if (!cnt_in) TRY(p->cnt.alloc(nctas * tie_warps * (size_t)RankSmem::cnt_words(G)));
+    TRY(p->cnt.alloc(nctas * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
 
     RankArgs& a = p->ra;
     a.data = m->data.p;
@@ -356,6 +337,8 @@ int configure_rank(hpdex_plan* p) {
     a.n1 = p->n1.p;
     a.n2 = p->n2.p;
     a.err = p->err.p;
+    a.dk_global = p->dk.p;
+    a.dg_global = p->dg.p;
     a.ek_global = p->ek.p;
     a.eg_global = p->eg.p;
     a.slice = slice;
@@ -513,12 +496,12 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
     if (mode == HPDEX_MODE_BATCHED) {
         CUDA_TRY(cudaMemsetAsync(p->queue.p, 0, sizeof(int32_t), s));
         p->ra.single_gene = -1;
-        TRY(dispatch_dtype<RankLaunch>(p->m->dtype, p, dim3(p->rank_grid), s));
+        TRY(rank_status(rank_launch(p->m->dtype, p->ra, p->rank_grid, p->rank_smem, s), "rank kernel launch"));
         *launches += 1;
     } else {
         for (long long c = 0; c < p->m->n_cols; ++c) {
             p->ra.single_gene = (int32_t)c;
-            TRY(dispatch_dtype<RankLaunch>(p->m->dtype, p, dim3(1), s));
+            TRY(rank_status(rank_launch(p->m->dtype, p->ra, 1, p->rank_smem, s), "rank kernel launch"));
             *launches += 1;
         }
         p->ra.single_gene = -1;
@@ -880,16 +863,6 @@ struct NoAllocKeyRange {
         return HPDEX_OK;
     }
 };
-template <class V>
-struct NoAllocRank {
-    static int run(const RankArgs* a, int grid, size_t smem, cudaStream_t s) {
-        auto k = mwu_rank_kernel<V, kRankThreads>;
-        k<<<grid, kRankThreads, smem, s>>>(*a);
-        CUDA_TRY(cudaGetLastError());
-        return HPDEX_OK;
-    }
-};
-
 }  // namespace
 
 extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, const int32_t* d_rows,
@@ -969,35 +942,37 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
             if (rows_host[g] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %d at column 0", g);
     }
 
-    // rank-kernel layout (same sizing rule as the plan path); accumulators and run counters
-    // must fit in shared memory here, which kNoAllocMaxGroups guarantees
+    // rank-kernel layout (same sizing rule as the plan path); the accumulators must fit in
+    // shared memory here, which kNoAllocMaxGroups guarantees
     const int nbl = 13;
     const size_t budget = std::min(nd->info.smem_per_sm - nd->info.smem_reserved, nd->info.smem_optin) - 2048;
-    int tie_warps = kRankThreads / 32;
+    const int tie_warps = kRankThreads / 32;
     RankSmem L(nbl, G, tie_warps, 1, 1, 0, kb);
-    while (L.total > budget && tie_warps > 4) {
-        tie_warps /= 2;
-        L = RankSmem(nbl, G, tie_warps, 1, 1, 0, kb);
-    }
-    if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: layout does not fit");
-    int cap = (int)std::min<size_t>((budget - L.total) / (kb + 4), (size_t)1 << 30);
+    if (L.total + 16384 > budget) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: layout does not fit");
+    int cap = (int)std::min<size_t>((budget - L.total) / (kb + 5), (size_t)1 << 30);
     cap = std::max(0, cap - 8);
     L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
     int blocks = 0;
-    TRY(dispatch_dtype<RankOccupancy>(dtype, L.total, nd->info.smem_optin, &blocks));
+    TRY(rank_status(rank_occupancy(dtype, L.total, nd->info.smem_optin, 1, &blocks), "rank kernel set-up"));
     if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM");
     const int grid = nd->info.sms * blocks;
-    long long slice = 0;
-    if ((long long)longest > cap) {
-        const size_t left = off < kNoAllocScratchBytes ? kNoAllocScratchBytes - off - 256 * (size_t)grid : 0;
-        slice = (long long)(left / ((size_t)grid * (kb + 4)));
-        if ((long long)longest > slice)
-            return fail(HPDEX_ERR_UNSUPPORTED,
-                        "hpdex_mannwhitneyu_noalloc: a column holds %llu entries, above the %lld the "
-                        "fixed scratch allows at this size", longest, slice);
-    }
-    void* ek = slice ? take((size_t)grid * slice * kb) : nullptr;
-    uint32_t* eg = slice ? reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4)) : nullptr;
+    // per CTA and warp: run counters (packed, and 32-bit for very large buckets)
+    uint32_t* cnt_glob = reinterpret_cast<uint32_t*>(
+        take(sizeof(uint32_t) * (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
+    if (off > kNoAllocScratchBytes) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: scratch exhausted");
+    // per CTA: a decoded copy of the current column and, for columns larger than the
+    // shared-memory capacity, a bucket-ordered slab slice
+    const int nslices = (long long)longest > cap ? 2 : 1;
+    const size_t left = off + 512 * (size_t)grid < kNoAllocScratchBytes ? kNoAllocScratchBytes - off - 512 * (size_t)grid : 0;
+    const long long slice = (long long)(left / ((size_t)grid * nslices * (kb + 4))) & ~7ll;
+    if ((long long)longest + 8 > slice)
+        return fail(HPDEX_ERR_UNSUPPORTED,
+                    "hpdex_mannwhitneyu_noalloc: a column holds %llu entries, above the %lld the "
+                    "fixed scratch allows at this size", longest, slice - 8);
+    void* dk = take((size_t)grid * slice * kb);
+    uint32_t* dg = reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4));
+    void* ek = nslices == 2 ? take((size_t)grid * slice * kb) : nullptr;
+    uint32_t* eg = nslices == 2 ? reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4)) : nullptr;
 
     TRY(dispatch_dtype<NoAllocKeyRange>(dtype, d_data, d_indptr, (int32_t)C, kmin, kmax, has_zero, s));
     RankArgs a{};
@@ -1022,17 +997,19 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     a.n1 = n1;
     a.n2 = n2;
     a.err = err;
+    a.dk_global = dk;
+    a.dg_global = dg;
     a.ek_global = ek;
     a.eg_global = eg;
-    a.slice = std::max<long long>(slice, 1);
+    a.slice = slice;
     a.acc_global = nullptr;
-    a.cnt_global = nullptr;
+    a.cnt_global = cnt_glob;
     a.nb_max_log2 = nbl;
     a.elem_smem_cap = cap;
     a.acc_in_smem = 1;
     a.cnt_in_smem = 1;
     a.tie_warps = tie_warps;
-    TRY(dispatch_dtype<NoAllocRank>(dtype, &a, grid, L.total, s));
+    TRY(rank_status(rank_launch(dtype, a, grid, L.total, s), "rank kernel launch"));
 
     PArgs pa{};
     pa.U1 = d_U1;

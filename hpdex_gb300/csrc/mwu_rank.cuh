@@ -11,18 +11,22 @@
 // slice for every target: reference ranks come from one bucket index per gene.
 //
 // Per gene:
-//   pass 1  (HBM) 4-wide vector loads of row ids and values; group id gather; value-bucket
-//           histograms of all stored elements and of reference elements (bucket = top bits
-//           of the key minus the column's minimum key, from the resident matrix's column
+//   pass 1  (HBM) 4-wide vector loads of row ids and values, group id gather, decode to
+//           (key, group) written at the entry's position in the CTA's scratch slice;
+//           value-bucket histograms of all stored elements and of reference elements
+//           (bucket = top bits of key - column minimum key, from the resident matrix's column
 //           key ranges); per-group stored counts (and negatives for zero_handling=mix)
 //   scan    exclusive prefix sums -> bucket start, reference count below each bucket
-//   pass 2  (L2)  scatter (key, group) into bucket order: shared memory when the gene fits,
-//           else the CTA's slice of a global scratch buffer (L2-resident)
-//   rank    singleton buckets: one atomic; buckets <= kSmallBucket: each element scans its
-//           bucket; larger buckets: a warp takes the bucket, extracts its distinct keys in
-//           ascending order (repeated warp minimum), and resolves each run of equal keys
-//           with per-warp group counters: one representative per (run, target) adds
-//           s*(2*lref + c0) and (c0+s)^3-(c0+s)-(c0^3-c0)
+//   slabs   consecutive bucket ranges holding at most the shared-memory element capacity;
+//           per slab:
+//   pass 2  (L2) scatter the slab's decoded elements into bucket order in shared memory (a
+//           slab made of one bucket larger than half the capacity uses a global slice)
+//   rank    32-bucket chunks to all warps: singleton buckets add one term; buckets of 2..8
+//           elements are resolved four at a time per warp, 9..32 one per warp, both with
+//           warp match instructions (equal keys, equal (key, group)); larger buckets go to a
+//           list that warps drain one bucket at a time with per-warp group counters: one
+//           representative per (run of equal keys, target) adds s*(2*lref + c0) to A and
+//           (c0+s)^3-(c0+s)-(c0^3-c0) to B
 //   final   zero block, U1, tie sum per target
 //
 // "Stored" elements are what the reference gathers into its slices (mannwhitneyu.cpp:
@@ -61,31 +65,41 @@ struct RankArgs {
     unsigned long long* err;   // [0]: min(gene*G + group) of a too-small sample (none)
                                // [1]: min(gene*G + group) of a group with more stored
                                //      entries than rows (duplicate row ids)
-    // global scratch, one slice of `slice` elements per CTA
-    void* ek_global;
+    // global scratch, one slice of `slice` elements per CTA for each of:
+    void* dk_global;           // decoded keys of the current gene, at the entries' positions
+    uint32_t* dg_global;       // decoded groups (kInvalid: not stored)
+    void* ek_global;           // bucket-ordered elements of a slab too big for shared memory
     uint32_t* eg_global;
-    long long slice;
+    long long slice;           // >= longest column + 4, multiple of 8
     unsigned char* acc_global; // per CTA 24*G bytes when the accumulators are not in SMEM
-    uint32_t* cnt_global;      // per CTA tie_warps * G counters when not in SMEM
+    uint32_t* cnt_global;      // per CTA and warp: packed counters (when not in SMEM), then
+                               // G 32-bit counters (buckets of more than 65535 elements)
     int32_t nb_max_log2;       // bucket table capacity (power of two)
     int32_t elem_smem_cap;     // elements that fit in shared memory
-    int32_t acc_in_smem;
-    int32_t cnt_in_smem;
-    int32_t tie_warps;         // warps that resolve large buckets (each owns counters)
+    int32_t acc_in_smem;       // accumulators and packed run counters in shared memory
+    int32_t cnt_in_smem;       // (equal to acc_in_smem; kept for the layout arithmetic)
+    int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
 };
 
-constexpr int kSmallBucket = 8;
+constexpr int kSmallBucket = 8;    // 2..8: four buckets per warp round
+constexpr int kMediumBucket = 32;  // 9..32: one warp round
 constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum per bucket
+constexpr uint32_t kInvalid = 0xffffffffu;
 
-// Shared-memory layout shared by host (sizing) and device (carving).
+// Shared-memory layout shared by host (sizing) and device (carving): bucket starts and
+// reference counts (NB + 1 each), the slab's list of large buckets, accumulators, run
+// counters, elements.
 struct RankSmem {
     size_t hist_bytes, acc_bytes, cnt_bytes, elem_bytes, total;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-    __host__ __device__ static int cnt_words(int G) { return G; }
+    __host__ __device__ static int cnt_words(int G) { return (G + 1) / 2; }
+    // a slab holds at most elem_cap elements outside one oversized bucket, so it has at most
+    // elem_cap / (kMediumBucket + 1) + 2 buckets above kMediumBucket
+    __host__ __device__ static int big_list(int elem_cap) { return elem_cap / 33 + 64; }
     __host__ __device__ RankSmem(int nb_max_log2, int G, int tie_warps, int acc_in_smem,
                                  int cnt_in_smem, int elem_cap, int key_bytes) {
         const size_t NB = size_t(1) << nb_max_log2;
-        hist_bytes = align16((3 * NB + 2) * 4);
+        hist_bytes = align16((2 * (NB + 1) + big_list(elem_cap)) * 4);
         acc_bytes = acc_in_smem ? align16(size_t(G) * 24) : 0;
         cnt_bytes = cnt_in_smem ? align16(size_t(tie_warps) * cnt_words(G) * 4) : 0;
         elem_bytes = align16(size_t(elem_cap) * (key_bytes + 4));
@@ -94,13 +108,17 @@ struct RankSmem {
 };
 
 template <int NT>
-__device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint32_t* wsy) {
-    // exclusive prefix sums of x[0..L) and y[0..L) in place; x[L], y[L] = totals
+__device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint32_t* wsy,
+                            uint32_t* xmax) {
+    // exclusive prefix sums of x[0..L) and y[0..L) in place; x[L], y[L] = totals;
+    // *xmax = max x[i] (the caller zeroes it before)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int per = (L + NT - 1) / NT;
     const int beg = min(L, tid * per), end = min(L, beg + per);
-    uint32_t sx = 0, sy = 0;
-    for (int i = beg; i < end; ++i) { sx += x[i]; sy += y[i]; }
+    uint32_t sx = 0, sy = 0, mx = 0;
+    for (int i = beg; i < end; ++i) { sx += x[i]; sy += y[i]; mx = max(mx, x[i]); }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0 && mx) atomicMax(xmax, mx);
     const uint32_t ix = warp_incl_scan(sx), iy = warp_incl_scan(sy);
     if (lane == 31) { wsx[warp] = ix; wsy[warp] = iy; }
     __syncthreads();
@@ -148,42 +166,30 @@ __device__ __forceinline__ void load4(const V* p, V (&v)[4]) {
     }
 }
 
-// Visits every (row, value) of [p0, p1) once: scalar head and tail, 4-wide aligned body,
-// two vectors per thread per iteration so that several loads and gathers are in flight.
-template <int NT, class V, class F>
-__device__ __forceinline__ void for_each_entry(const int32_t* rows, const V* data, long long p0,
-                                               long long p1, F&& f) {
-    const int tid = threadIdx.x;
-    long long a = (p0 + 3) & ~3ll;
-    if (a > p1) a = p1;
-    const long long b = a + ((p1 - a) & ~3ll);
-    for (long long p = p0 + tid; p < a; p += NT) f(rows[p], data[p]);
-    for (long long q = a + 4ll * tid; q < b; q += 8ll * NT) {
-        const long long q2 = q + 4ll * NT;
-        int4 r0 = __ldg(reinterpret_cast<const int4*>(rows + q));
-        V v0[4];
-        load4<V>(data + q, v0);
-        int4 r1 = make_int4(-1, -1, -1, -1);
-        V v1[4] = {V(0), V(0), V(0), V(0)};
-        const bool second = q2 < b;
-        if (second) {
-            r1 = __ldg(reinterpret_cast<const int4*>(rows + q2));
-            load4<V>(data + q2, v1);
-        }
-        f(r0.x, v0[0]); f(r0.y, v0[1]); f(r0.z, v0[2]); f(r0.w, v0[3]);
-        if (second) { f(r1.x, v1[0]); f(r1.y, v1[1]); f(r1.z, v1[2]); f(r1.w, v1[3]); }
+// 4 keys at a 4-aligned position (vector stores)
+template <class K>
+__device__ __forceinline__ void store4(K* p, const K (&k)[4]) {
+    if constexpr (sizeof(K) == 4) {
+        *reinterpret_cast<uint4*>(p) = make_uint4(k[0], k[1], k[2], k[3]);
+    } else {
+        reinterpret_cast<ulonglong2*>(p)[0] = make_ulonglong2(k[0], k[1]);
+        reinterpret_cast<ulonglong2*>(p)[1] = make_ulonglong2(k[2], k[3]);
     }
-    for (long long p = b + tid; p < p1; p += NT) f(rows[p], data[p]);
 }
 
-// per-warp, per-group counters of a run
-__device__ __forceinline__ void cnt_inc(uint32_t* cnt, uint32_t g) { atomicAdd(&cnt[g], 1u); }
+// Per-warp, per-group counters of a run, 16 bits each (two groups per 32-bit word). A run
+// never counts more than 65535 elements of one group here: buckets with more than 65535
+// elements are resolved with 32-bit counters instead.
+__device__ __forceinline__ void cnt_inc(uint32_t* cnt, uint32_t g) {
+    atomicAdd(&cnt[g >> 1], (g & 1u) ? 0x10000u : 1u);
+}
 __device__ __forceinline__ uint32_t cnt_take(uint32_t* cnt, uint32_t g) {
     // returns the count and clears it; only the first caller per group sees it nonzero
-    return atomicExch(&cnt[g], 0u);
+    const uint32_t old = atomicAnd(&cnt[g >> 1], (g & 1u) ? 0x0000ffffu : 0xffff0000u);
+    return (g & 1u) ? (old >> 16) : (old & 0xffffu);
 }
-
-constexpr uint32_t kRetired = 0xffffffffu;  // group id of an element already resolved
+__device__ __forceinline__ void cntw_inc(uint32_t* cnt, uint32_t g) { atomicAdd(&cnt[g], 1u); }
+__device__ __forceinline__ uint32_t cntw_take(uint32_t* cnt, uint32_t g) { return atomicExch(&cnt[g], 0u); }
 
 __device__ __forceinline__ unsigned long long tie_delta(unsigned long long c0,
                                                        unsigned long long s) {
@@ -191,103 +197,172 @@ __device__ __forceinline__ unsigned long long tie_delta(unsigned long long c0,
     return 3ull * c0 * c0 * s + 3ull * c0 * s * s + s * s * s - s;
 }
 
-// Resolves one run of equal keys inside a bucket: the live elements of [s0, s0+m) whose key
-// equals `key` (all of them when `pure`). lref = reference elements below the run, c0 =
-// reference elements in the run.
 template <class K>
-__device__ __forceinline__ void resolve_run(const K* ek, const uint32_t* eg, uint32_t s0, uint32_t m,
-                                            bool pure, K key, unsigned long long lref,
-                                            unsigned long long c0, unsigned long long* A,
-                                            unsigned long long* B, uint32_t* cnt,
-                                            unsigned long long& tref) {
-    const int lane = threadIdx.x & 31;
-    for (uint32_t j = lane; j < m; j += 32) {
-        const uint32_t g = eg[s0 + j];
-        if (g && g != kRetired && (pure || ek[s0 + j] == key)) cnt_inc(cnt, g);
-    }
-    __syncwarp();
-    const unsigned long long a = 2ull * lref + c0;
-    for (uint32_t j = lane; j < m; j += 32) {
-        const uint32_t g = eg[s0 + j];
-        if (g && g != kRetired && (pure || ek[s0 + j] == key)) {
-            const unsigned long long s = cnt_take(cnt, g);
-            if (s) {
-                atomicAdd(&A[g], s * a);
-                const unsigned long long tb = tie_delta(c0, s);
-                if (tb) atomicAdd(&B[g], tb);
-            }
-        }
-    }
-    __syncwarp();
-    if (lane == 0) tref += c0 * c0 * c0 - c0;
+__device__ __forceinline__ K wmin(unsigned mask, K v) {
+    if constexpr (sizeof(K) == 4) return __reduce_min_sync(mask, v);
+    else return warp_min(v);
+}
+template <class K>
+__device__ __forceinline__ K wmax(unsigned mask, K v) {
+    if constexpr (sizeof(K) == 4) return __reduce_max_sync(mask, v);
+    else return warp_max(v);
 }
 
-// Warp-level handling of a bucket with more than kSmallBucket elements.
+// Accumulator set of a gene: A (doubled U2 terms) and B (target tie terms) per group.
+struct Acc {
+    unsigned long long* A;
+    unsigned long long* B;
+};
+
+// Adds the contribution of s equal (key, target g) elements whose run has c0 reference
+// elements and lref reference elements below it.
+__device__ __forceinline__ void add_pair(const Acc& acc, uint32_t g, unsigned long long s,
+                                         unsigned long long lref, unsigned long long c0) {
+    atomicAdd(&acc.A[g], s * (2ull * lref + c0));
+    const unsigned long long tb = tie_delta(c0, s);
+    if (tb) atomicAdd(&acc.B[g], tb);
+}
+
+// One warp round over up to 32 elements of buckets that lie wholly inside the round:
+// lane L holds (key, g) when active; `sub` is the lane mask of L's bucket, rb its reference
+// count below. Equal keys and equal (key, group) come from warp match instructions; the
+// lowest lane of each (key, group) set adds the set's contribution.
 template <class K>
-__device__ void resolve_big_bucket(uint32_t b, const uint32_t* hall, const uint32_t* href,
-                                   const K* ek, uint32_t* eg, unsigned long long* A,
-                                   unsigned long long* B, uint32_t* cnt,
-                                   unsigned long long& tref) {
+__device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, unsigned sub,
+                                              uint32_t rb, const Acc& acc,
+                                              unsigned long long& tref) {
     const int lane = threadIdx.x & 31;
-    const uint32_t s0 = hall[b], m = hall[b + 1] - s0;
-    const uint32_t rb = href[b], c0b = href[b + 1] - rb;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) return;
+    const unsigned refm = __ballot_sync(0xffffffffu, active && g == 0u);
+    if (active) {
+        const unsigned mk = __match_any_sync(act, key) & sub;  // same key, same bucket
+        const unsigned mg = __match_any_sync(act, g);
+        const unsigned pair = mk & mg;
+        const uint32_t c0 = __popc(mk & refm);
+        const bool leader_key = (__ffs((int)mk) - 1) == lane;
+        // reference elements of my bucket with a smaller key: sum over the other keys'
+        // leaders (few: one per distinct key)
+        uint32_t lt = 0;
+        unsigned leaders = __ballot_sync(act, leader_key);
+        const bool impure_any = __any_sync(act, mk != (sub & act));
+        if (impure_any) {
+            while (leaders) {
+                const int j = __ffs((int)leaders) - 1;
+                leaders &= leaders - 1u;
+                const K kj = __shfl_sync(act, key, j);
+                const uint32_t cj = __shfl_sync(act, c0, j);
+                if (((sub >> j) & 1u) && kj < key) lt += cj;
+            }
+        }
+        if ((__ffs((int)pair) - 1) == lane) {
+            const uint32_t s = __popc(pair);
+            if (g) add_pair(acc, g, s, (unsigned long long)rb + lt, c0);
+            else tref += (unsigned long long)c0 * c0 * c0 - c0;  // s == c0 for the reference
+        }
+    }
+}
+
+// Warp-level resolution of a bucket of more than kMediumBucket elements [s0, s0+m).
+// Pass A counts the targets per group assuming the bucket is pure (one key) while finding
+// its key range and reference count; pure buckets finish with pass B (one representative
+// per group adds the contribution). Impure buckets undo the counts and visit their distinct
+// keys in ascending order (warp minimum), two passes per key; after kMaxRunsByMin keys the
+// rest is resolved element by element. Counters are zero on entry and on exit.
+template <class K, bool WIDE, class EK, class EG>
+__device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, const EG* eg,
+                            const Acc& acc, uint32_t* cnt, unsigned long long& tref) {
+    const int lane = threadIdx.x & 31;
     K lo = ~K(0), hi = K(0);
+    uint32_t c0 = 0;
     for (uint32_t j = lane; j < m; j += 32) {
         const K k = ek[s0 + j];
+        const uint32_t g = eg[s0 + j];
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
+        if (g) {
+            if (WIDE) cntw_inc(cnt, g); else cnt_inc(cnt, g);
+        } else {
+            ++c0;
+        }
     }
-    lo = warp_min(lo);
-    hi = warp_max(hi);
-    if (lo == hi) {  // pure bucket: a single run
-        resolve_run<K>(ek, eg, s0, m, true, lo, rb, c0b, A, B, cnt, tref);
+    lo = wmin<K>(0xffffffffu, lo);
+    hi = wmax<K>(0xffffffffu, hi);
+    c0 = __reduce_add_sync(0xffffffffu, c0);
+    __syncwarp();
+    if (lo == hi) {
+        for (uint32_t j = lane; j < m; j += 32) {
+            const uint32_t g = eg[s0 + j];
+            if (g) {
+                const uint32_t s = WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g);
+                if (s) add_pair(acc, g, s, rb, c0);
+            }
+        }
+        if (lane == 0) tref += (unsigned long long)c0 * c0 * c0 - c0;
+        __syncwarp();
         return;
     }
-    // impure: distinct keys in ascending order by repeated warp minimum; resolved elements
-    // are retired through their group id (the bucket's slice is private to this warp)
+    // impure: clear the counts, then one key at a time
+    for (uint32_t j = lane; j < m; j += 32) {
+        const uint32_t g = eg[s0 + j];
+        if (g) (void)(WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g));
+    }
+    __syncwarp();
     unsigned long long lref = rb;
     K cur = lo;
     for (int it = 0;; ++it) {
-        uint32_t c0 = 0;  // reference elements in the current run
-        for (uint32_t j = lane; j < m; j += 32) c0 += (eg[s0 + j] == 0u && ek[s0 + j] == cur);
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, d);
-        resolve_run<K>(ek, eg, s0, m, false, cur, lref, c0, A, B, cnt, tref);
-        lref += c0;
-        // retire the run and find the next key
-        K nxt = ~K(0);
-        bool any = false;
+        uint32_t r0 = 0;
         for (uint32_t j = lane; j < m; j += 32) {
+            if (ek[s0 + j] != cur) continue;
             const uint32_t g = eg[s0 + j];
-            if (g == kRetired) continue;
-            const K k = ek[s0 + j];
-            if (k == cur) { eg[s0 + j] = kRetired; continue; }
-            nxt = k < nxt ? k : nxt;
-            any = true;
+            if (g) {
+                if (WIDE) cntw_inc(cnt, g); else cnt_inc(cnt, g);
+            } else {
+                ++r0;
+            }
         }
-        nxt = warp_min(nxt);
-        any = __any_sync(0xffffffffu, any);
+        r0 = __reduce_add_sync(0xffffffffu, r0);
         __syncwarp();
-        if (!any) break;
+        K nxt = ~K(0);
+        bool more = false;
+        for (uint32_t j = lane; j < m; j += 32) {
+            const K k = ek[s0 + j];
+            if (k == cur) {
+                const uint32_t g = eg[s0 + j];
+                if (g) {
+                    const uint32_t s = WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g);
+                    if (s) add_pair(acc, g, s, lref, r0);
+                }
+            } else if (k > cur) {
+                nxt = k < nxt ? k : nxt;
+                more = true;
+            }
+        }
+        if (lane == 0) tref += (unsigned long long)r0 * r0 * r0 - r0;
+        lref += r0;
+        more = __any_sync(0xffffffffu, more);
+        nxt = wmin<K>(0xffffffffu, nxt);
+        __syncwarp();
+        if (!more) break;
         if (it + 1 >= kMaxRunsByMin) {
-            // many distinct keys (continuous data): finish by brute force per element
+            // many distinct keys (continuous data): the elements with key >= nxt one by one
             for (uint32_t i = lane; i < m; i += 32) {
-                const uint32_t g = eg[s0 + i];
-                if (g == kRetired) continue;
                 const K k = ek[s0 + i];
-                uint32_t lt = 0, e0 = 0, s = 0;
+                if (k < nxt) continue;
+                const uint32_t g = eg[s0 + i];
+                uint32_t lt = 0, e0 = 0, sc = 0;
                 for (uint32_t j = 0; j < m; ++j) {
-                    const uint32_t gj = eg[s0 + j];
-                    if (gj == kRetired) continue;
                     const K kj = ek[s0 + j];
+                    if (kj < nxt) continue;
+                    const uint32_t gj = eg[s0 + j];
                     if (gj == 0u) { lt += (kj < k); e0 += (kj == k); }
-                    s += (gj == g && kj == k);
+                    sc += (gj == g && kj == k);
                 }
                 if (g) {
-                    atomicAdd(&A[g], 2ull * (lref + lt) + e0);
-                    const unsigned long long cc = e0, ss = s;
+                    atomicAdd(&acc.A[g], 2ull * (lref + lt) + e0);
+                    const unsigned long long cc = e0, ss = sc;
                     const unsigned long long tb = 3ull * cc * cc + 3ull * cc * ss + ss * ss - 1ull;
-                    if (tb) atomicAdd(&B[g], tb);
+                    if (tb) atomicAdd(&acc.B[g], tb);
                 } else {
                     tref += (unsigned long long)e0 * e0 - 1ull;
                 }
@@ -299,45 +374,150 @@ __device__ void resolve_big_bucket(uint32_t b, const uint32_t* hall, const uint3
     }
 }
 
-template <class V, int NT>
+// Rank phase of one slab: elements [0, cnt) in bucket order in ek/eg, buckets [blo, bhi)
+// starting at `base` in the gene's bucket order.
+template <class K, class EK, class EG>
+__device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi, uint32_t base,
+                          const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
+                          uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
+                          uint32_t* s_bigi, const Acc& acc, uint32_t* cnt, uint32_t* wide_cnt,
+                          unsigned long long& tref) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nchunks = (bhi - blo + 31u) / 32u;
+    for (;;) {
+        uint32_t ch = 0;
+        if (lane == 0) ch = atomicAdd(s_chunk, 1u);
+        ch = __shfl_sync(0xffffffffu, ch, 0);
+        if (ch >= nchunks) break;
+        const uint32_t b = blo + 32u * ch + lane;
+        uint32_t sb = 0, m = 0, rb = 0;
+        if (b < bhi) {
+            sb = (b == blo) ? base : hall[b - 1];
+            m = hall[b] - sb;
+            rb = href[b];
+        }
+        const uint32_t s0 = sb - base;
+        if (m == 1u) {
+            const uint32_t g = eg[s0];
+            if (g) atomicAdd(&acc.A[g], 2ull * rb);  // a lone target value: no reference tie
+        }
+        bool spill = false;
+        if (m > (uint32_t)kMediumBucket) {
+            const uint32_t slot = atomicAdd(s_nbig, 1u);
+            if (slot < biglist_cap) biglist[slot] = b;
+            else spill = true;  // list full (the sizing rules this out): resolve below
+        }
+        // buckets of 2..8 elements: four per round, 8 lanes each
+        unsigned smask = __ballot_sync(0xffffffffu, m >= 2u && m <= (uint32_t)kSmallBucket);
+        while (smask) {
+            int src[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                src[q] = smask ? __ffs((int)smask) - 1 : -1;
+                if (smask) smask &= smask - 1u;
+            }
+            const int q = lane >> 3, e = lane & 7;
+            const int sl = src[q];
+            const uint32_t mq = __shfl_sync(0xffffffffu, m, sl < 0 ? 0 : sl);
+            const uint32_t sq = __shfl_sync(0xffffffffu, s0, sl < 0 ? 0 : sl);
+            const uint32_t rq = __shfl_sync(0xffffffffu, rb, sl < 0 ? 0 : sl);
+            const bool active = sl >= 0 && (uint32_t)e < mq;
+            K key = K(0);
+            uint32_t g = 0;
+            if (active) { key = ek[sq + e]; g = eg[sq + e]; }
+            resolve_round<K>(active, key, g, 0xffu << (8 * q), rq, acc, tref);
+        }
+        // buckets of 9..32 elements: one round each
+        unsigned mmask = __ballot_sync(0xffffffffu, m > (uint32_t)kSmallBucket && m <= (uint32_t)kMediumBucket);
+        while (mmask) {
+            const int j = __ffs((int)mmask) - 1;
+            mmask &= mmask - 1u;
+            const uint32_t mj = __shfl_sync(0xffffffffu, m, j);
+            const uint32_t sj = __shfl_sync(0xffffffffu, s0, j);
+            const uint32_t rj = __shfl_sync(0xffffffffu, rb, j);
+            const bool active = (uint32_t)lane < mj;
+            K key = K(0);
+            uint32_t g = 0;
+            if (active) { key = ek[sj + lane]; g = eg[sj + lane]; }
+            resolve_round<K>(active, key, g, 0xffffffffu, rj, acc, tref);
+        }
+        unsigned over = __ballot_sync(0xffffffffu, spill);
+        while (over) {
+            const int j = __ffs((int)over) - 1;
+            over &= over - 1u;
+            const uint32_t mj = __shfl_sync(0xffffffffu, m, j);
+            const uint32_t sj = __shfl_sync(0xffffffffu, s0, j);
+            const uint32_t rj = __shfl_sync(0xffffffffu, rb, j);
+            if (mj <= 65535u) resolve_big<K, false>(sj, mj, rj, ek, eg, acc, cnt, tref);
+            else resolve_big<K, true>(sj, mj, rj, ek, eg, acc, wide_cnt, tref);
+        }
+    }
+    __syncthreads();
+    const uint32_t nbig = min(*s_nbig, biglist_cap);
+    for (;;) {
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(s_bigi, 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= nbig) break;
+        const uint32_t b = biglist[q];
+        const uint32_t sb = (b == blo) ? base : hall[b - 1];
+        const uint32_t m = hall[b] - sb;
+        if (m <= 65535u) resolve_big<K, false>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
+        else resolve_big<K, true>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
+    }
+}
+
+template <class V, int NT, bool ACC_SMEM>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_gene;
     __shared__ unsigned long long s_tref;
-    __shared__ uint32_t s_nbig;
+    __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi;
     __shared__ uint32_t s_wsx[32], s_wsy[32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = a.G, zh = a.zero_handling;
     const int NBMAX = 1 << a.nb_max_log2;
-    const RankSmem L(a.nb_max_log2, G, a.tie_warps, a.acc_in_smem, a.cnt_in_smem,
-                     a.elem_smem_cap, (int)sizeof(K));
+    const RankSmem L(a.nb_max_log2, G, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,
+                     (int)sizeof(K));
     const int cw = RankSmem::cnt_words(G);
 
-    uint32_t* hall = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* href = hall + NBMAX + 1;
-    uint32_t* cursor = href + NBMAX + 1;
-    unsigned char* accb = a.acc_in_smem ? smem + L.hist_bytes
-                                        : a.acc_global + (size_t)blockIdx.x * 24 * G;
+    uint32_t* hall = reinterpret_cast<uint32_t*>(smem);  // bucket start (after the scan)
+    uint32_t* href = hall + NBMAX + 1;                   // reference elements below a bucket
+    uint32_t* biglist = href + NBMAX + 1;                // large buckets of the current slab
+    const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(a.elem_smem_cap);
+    unsigned char* accb;
+    uint32_t* cnt_base;
+    uint32_t* cnt_glob = a.cnt_global + (size_t)blockIdx.x * a.tie_warps * (cw + G);
+    if constexpr (ACC_SMEM) {
+        accb = smem + L.hist_bytes;
+        cnt_base = reinterpret_cast<uint32_t*>(smem + L.hist_bytes + L.acc_bytes);
+    } else {
+        accb = a.acc_global + (size_t)blockIdx.x * 24 * G;
+        cnt_base = cnt_glob;
+    }
     unsigned long long* A = reinterpret_cast<unsigned long long*>(accb);
     unsigned long long* B = A + G;
     uint32_t* nz = reinterpret_cast<uint32_t*>(B + G);
     uint32_t* ng = nz + G;
-    uint32_t* cnt_base = a.cnt_in_smem
-                             ? reinterpret_cast<uint32_t*>(smem + L.hist_bytes + L.acc_bytes)
-                             : a.cnt_global + (size_t)blockIdx.x * a.tie_warps * cw;
+    const Acc acc{A, B};
+    uint32_t* wide_base = cnt_glob + (size_t)a.tie_warps * cw;
+    uint32_t* cnt = cnt_base + (size_t)warp * cw;
+    uint32_t* wide_cnt = wide_base + (size_t)warp * G;
     K* ek_s = reinterpret_cast<K*>(smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes);
     uint32_t* eg_s = reinterpret_cast<uint32_t*>(ek_s + a.elem_smem_cap);
+    K* dk = reinterpret_cast<K*>(a.dk_global) + (size_t)blockIdx.x * a.slice;
+    uint32_t* dg = a.dg_global + (size_t)blockIdx.x * a.slice;
     K* ek_g = reinterpret_cast<K*>(a.ek_global) + (size_t)blockIdx.x * a.slice;
     uint32_t* eg_g = a.eg_global + (size_t)blockIdx.x * a.slice;
 
-    const V* data = reinterpret_cast<const V*>(a.data);
-    const int32_t* rows = a.rows;
     const int32_t* gidp = a.gid;
-    const long long nrows = a.n_rows;
+    const uint32_t nrows = (uint32_t)a.n_rows;
 
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
+    for (int i = tid; i < a.tie_warps * G; i += NT) wide_base[i] = 0u;
+    if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
 
     bool first = true;
     for (;;) {
@@ -351,14 +531,22 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             }
             s_gene = c;
             s_tref = 0ull;
-            s_nbig = 0u;
+            s_maxb = 0u;
         }
         first = false;
         for (int g = tid; g < G; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
         __syncthreads();
         const int c = s_gene;
         if (c < 0) break;
-        const long long p0 = a.indptr[c], p1 = a.indptr[c + 1];
+        const long long p0 = a.indptr[c];
+        const uint32_t nraw = (uint32_t)(a.indptr[c + 1] - p0);
+        // entries of this gene, re-based: entry i is rows[i], data[i]; the decoded copy of
+        // entry i sits at dk/dg[i + off] where off = p0 % 4 keeps vector accesses aligned
+        const int32_t* rows = a.rows + p0;
+        const V* data = reinterpret_cast<const V*>(a.data) + p0;
+        const uint32_t off = (uint32_t)(p0 & 3);
+        const uint32_t ia = min(nraw, (4u - off) & 3u);           // aligned body [ia, ib)
+        const uint32_t ib = ia + ((nraw - ia) & ~3u);
 
         // ---- bucket function from the column's key range ----
         K kmin = (K)a.col_kmin[c], kmax = (K)a.col_kmax[c];
@@ -367,9 +555,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             kmin = kz < kmin ? kz : kmin;
             kmax = kz > kmax ? kz : kmax;
         }
-        const long long nraw = p1 - p0;
         int nbl = 1;
-        while (nbl < a.nb_max_log2 && (1ll << nbl) < 2 * nraw) ++nbl;
+        while (nbl < a.nb_max_log2 && (1u << nbl) < 2u * nraw) ++nbl;
         const int NB = 1 << nbl;
         int shift = 0;
         if (kmin <= kmax) {
@@ -379,84 +566,151 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         for (int b = tid; b <= NB; b += NT) { hall[b] = 0u; href[b] = 0u; }
         __syncthreads();
 
-        // ---- pass 1: histograms and per-group stored counts ----
+        // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
-        for_each_entry<NT, V>(rows, data, p0, p1, [&](int32_t r, V v) {
-            if (r < 0 || (long long)r >= nrows) return;
+        auto decode = [&](int32_t r, V v, K& key) -> uint32_t {
+            if ((uint32_t)r >= nrows) return kInvalid;  // negative ids wrap above n_rows
             const int g = __ldg(gidp + r);
-            if (g < 0 || g >= G) return;
-            if (!Val<V>::finite(v)) return;
-            if (zh != ZH_NONE && Val<V>::zero(v)) return;
+            if ((unsigned)g >= (unsigned)G) return kInvalid;
+            if (!Val<V>::finite(v)) return kInvalid;
+            if (zh != ZH_NONE && Val<V>::zero(v)) return kInvalid;
+            key = Val<V>::key(v);
+            return (uint32_t)g;
+        };
+        auto count = [&](uint32_t g, K key, V v) {
             if (g) atomicAdd(&nz[g], 1u);
             else ++nref_local;
             if (zh == ZH_MIX && Val<V>::neg(v)) atomicAdd(&ng[g], 1u);
-            const uint32_t b = (uint32_t)((Val<V>::key(v) - kmin) >> shift);
+            const uint32_t b = (uint32_t)((key - kmin) >> shift);
             atomicAdd(&hall[b], 1u);
             if (g == 0) atomicAdd(&href[b], 1u);
-        });
-        for (int d = 16; d > 0; d >>= 1) nref_local += __shfl_xor_sync(0xffffffffu, nref_local, d);
-        if (lane == 0 && nref_local) atomicAdd(&nz[0], nref_local);
-        __syncthreads();
-        block_scan2<NT>(hall, href, NB, s_wsx, s_wsy);
-        const uint32_t n = hall[NB];
-        for (int b = tid; b < NB; b += NT) cursor[b] = hall[b];
-        const bool in_smem = n <= (uint32_t)a.elem_smem_cap;
-        K* ek = in_smem ? ek_s : ek_g;
-        uint32_t* eg = in_smem ? eg_s : eg_g;
-        __syncthreads();
-
-        // ---- pass 2: scatter into bucket order ----
-        for_each_entry<NT, V>(rows, data, p0, p1, [&](int32_t r, V v) {
-            if (r < 0 || (long long)r >= nrows) return;
-            const int g = __ldg(gidp + r);
-            if (g < 0 || g >= G) return;
-            if (!Val<V>::finite(v)) return;
-            if (zh != ZH_NONE && Val<V>::zero(v)) return;
-            const K k = Val<V>::key(v);
-            const uint32_t b = (uint32_t)((k - kmin) >> shift);
-            const uint32_t pos = atomicAdd(&cursor[b], 1u);
-            ek[pos] = k;
-            eg[pos] = (uint32_t)g;
-        });
-        __syncthreads();
-
-        // ---- rank: singletons and small buckets per element ----
-        unsigned long long tref = 0ull;
-        for (uint32_t i = tid; i < n; i += NT) {
-            const K k = ek[i];
-            const uint32_t g = eg[i];
-            const uint32_t b = (uint32_t)((k - kmin) >> shift);
-            const uint32_t s0 = hall[b], m = hall[b + 1] - s0, rb = href[b];
-            if (m == 1) {
-                if (g) atomicAdd(&A[g], 2ull * rb);
-            } else if (m <= (uint32_t)kSmallBucket) {
-                uint32_t lt = 0, c0 = 0, s = 0;
-                for (uint32_t j = s0; j < s0 + m; ++j) {
-                    const K kj = ek[j];
-                    const uint32_t gj = eg[j];
-                    if (gj == 0u) { lt += (kj < k); c0 += (kj == k); }
-                    s += (gj == g && kj == k);
+        };
+        auto scalar1 = [&](uint32_t i) {
+            K key = K(0);
+            const V v = data[i];
+            const uint32_t g = decode(rows[i], v, key);
+            dk[i + off] = key;
+            dg[i + off] = g;
+            if (g != kInvalid) count(g, key, v);
+        };
+        for (uint32_t i = tid; i < ia; i += NT) scalar1(i);
+        {
+            uint32_t q = ia + 4u * tid;
+            if (q < ib) {
+                int4 r = __ldg(reinterpret_cast<const int4*>(rows + q));
+                V v[4];
+                load4<V>(data + q, v);
+                for (;;) {
+                    const uint32_t qn = q + 4u * NT;
+                    const bool more = qn < ib;
+                    int4 rn = make_int4(-1, -1, -1, -1);
+                    V vn[4] = {V(0), V(0), V(0), V(0)};
+                    if (more) {
+                        rn = __ldg(reinterpret_cast<const int4*>(rows + qn));
+                        load4<V>(data + qn, vn);
+                    }
+                    const int32_t rr[4] = {r.x, r.y, r.z, r.w};
+                    K key[4] = {K(0), K(0), K(0), K(0)};
+                    uint32_t g[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) g[k] = decode(rr[k], v[k], key[k]);
+                    store4<K>(dk + q + off, key);
+                    *reinterpret_cast<uint4*>(dg + q + off) = make_uint4(g[0], g[1], g[2], g[3]);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (g[k] != kInvalid) count(g[k], key[k], v[k]);
+                    if (!more) break;
+                    q = qn;
+                    r = rn;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[k] = vn[k];
                 }
-                if (g) {
-                    atomicAdd(&A[g], 2ull * (rb + lt) + c0);
-                    const unsigned long long cc = c0, ss = s;
-                    const unsigned long long tb = 3ull * cc * cc + 3ull * cc * ss + ss * ss - 1ull;
-                    if (tb) atomicAdd(&B[g], tb);
-                } else {
-                    tref += (unsigned long long)c0 * c0 - 1ull;
-                }
-            } else if (i == s0) {
-                cursor[atomicAdd(&s_nbig, 1u)] = b;
             }
         }
-        __syncthreads();  // the big-bucket list in `cursor` is complete
+        for (uint32_t i = ib + tid; i < nraw; i += NT) scalar1(i);
+        nref_local = __reduce_add_sync(0xffffffffu, nref_local);
+        if (lane == 0 && nref_local) atomicAdd(&nz[0], nref_local);
+        __syncthreads();
+        block_scan2<NT>(hall, href, NB, s_wsx, s_wsy, &s_maxb);
+        const uint32_t n = hall[NB];
+        const uint32_t cap = (uint32_t)a.elem_smem_cap;
+        // slabs: buckets whose start offset lies in [k*W, (k+1)*W) form slab k; a slab holds
+        // at most W + (largest bucket) elements, which fits the shared-memory capacity unless a
+        // single bucket is larger than half of it (then that slab uses the global slice)
+        const uint32_t maxb = s_maxb;
+        uint32_t W;
+        if (cap < 1024u) {
+            W = max(n, 1u);  // (almost) no shared memory for elements: one slab, global slice
+        } else {
+            W = cap > maxb ? cap - maxb : 0u;
+            W = max(W, cap / 2u);
+        }
+        const uint32_t nslabs = n ? (n - 1u) / W + 1u : 0u;
 
-        // ---- rank: big buckets, one warp each ----
-        if (warp < a.tie_warps) {
-            uint32_t* cnt = cnt_base + (size_t)warp * cw;
-            const uint32_t nbig = s_nbig;
-            for (uint32_t q = warp; q < nbig; q += a.tie_warps)
-                resolve_big_bucket<K>(cursor[q], hall, href, ek, eg, A, B, cnt, tref);
+        // During a slab's scatter hall[b] counts up from the start to the end of bucket b,
+        // so afterwards the start of bucket b is hall[b - 1] (or the slab base for its first
+        // bucket) and buckets of later slabs still hold their starts.
+        unsigned long long tref = 0ull;
+        uint32_t blo = 0;
+        for (uint32_t slab = 0; slab < nslabs; ++slab) {
+            if (tid == 0) {
+                uint32_t lo = blo, hi = (uint32_t)NB;
+                const uint32_t t1 = (slab + 1u) * W;
+                while (lo < hi) { const uint32_t mid = (lo + hi) >> 1; if (hall[mid] < t1) lo = mid + 1; else hi = mid; }
+                s_slab_hi = (slab + 1u == nslabs) ? (uint32_t)NB : lo;
+            }
+            __syncthreads();
+            const uint32_t bhi = s_slab_hi;
+            const uint32_t base = hall[blo], cnt_slab = hall[bhi] - base;
+            const bool in_smem = cnt_slab <= cap;
+
+            // ---- pass 2 (L2): scatter this slab's decoded elements into bucket order ----
+            if (cnt_slab) {
+                auto place = [&](K key, uint32_t g) {
+                    if (g == kInvalid) return;
+                    const uint32_t b = (uint32_t)((key - kmin) >> shift);
+                    if (b < blo || b >= bhi) return;
+                    const uint32_t pos = atomicAdd(&hall[b], 1u) - base;
+                    if (in_smem) { ek_s[pos] = key; eg_s[pos] = g; }
+                    else { ek_g[pos] = key; eg_g[pos] = g; }
+                };
+                for (uint32_t i = tid; i < ia; i += NT) place(dk[i + off], dg[i + off]);
+                uint32_t q = ia + 4u * tid;
+                if (q < ib) {
+                    K k4[4];
+                    load4<K>(dk + q + off, k4);
+                    uint4 g4 = *reinterpret_cast<const uint4*>(dg + q + off);
+                    for (;;) {
+                        const uint32_t qn = q + 4u * NT;
+                        const bool more = qn < ib;
+                        K kn[4] = {K(0), K(0), K(0), K(0)};
+                        uint4 gn = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
+                        if (more) {
+                            load4<K>(dk + qn + off, kn);
+                            gn = *reinterpret_cast<const uint4*>(dg + qn + off);
+                        }
+                        place(k4[0], g4.x); place(k4[1], g4.y); place(k4[2], g4.z); place(k4[3], g4.w);
+                        if (!more) break;
+                        q = qn;
+                        g4 = gn;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) k4[k] = kn[k];
+                    }
+                }
+                for (uint32_t i = ib + tid; i < nraw; i += NT) place(dk[i + off], dg[i + off]);
+            }
+            __syncthreads();
+
+            // ---- rank ----
+            if (in_smem)
+                rank_slab<K>(ek_s, eg_s, blo, bhi, base, hall, href, biglist, biglist_cap,
+                             &s_chunk, &s_nbig, &s_bigi, acc, cnt, wide_cnt, tref);
+            else
+                rank_slab<K>(ek_g, eg_g, blo, bhi, base, hall, href, biglist, biglist_cap,
+                             &s_chunk, &s_nbig, &s_bigi, acc, cnt, wide_cnt, tref);
+            __syncthreads();
+            if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
+            blo = bhi;
         }
         tref = warp_sum_u64(tref);
         if (lane == 0 && tref) atomicAdd(&s_tref, tref);
