@@ -610,10 +610,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                         load4<V>(data + qn, vn);
                     }
                     const int32_t rr[4] = {r.x, r.y, r.z, r.w};
-                    K key[4] = {K(0), K(0), K(0), K(0)};
+                    // all four group-id gathers in flight before any of them is tested
+                    int gl[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        gl[k] = __ldg(gidp + ((uint32_t)rr[k] < nrows ? rr[k] : 0));
+                    K key[4];
                     uint32_t g[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) g[k] = decode(rr[k], v[k], key[k]);
+                    for (int k = 0; k < 4; ++k) {
+                        const bool ok = (uint32_t)rr[k] < nrows && (unsigned)gl[k] < (unsigned)G &&
+                                        Val<V>::finite(v[k]) &&
+                                        (zh == ZH_NONE || !Val<V>::zero(v[k]));
+                        key[k] = ok ? Val<V>::key(v[k]) : K(0);
+                        g[k] = ok ? (uint32_t)gl[k] : kInvalid;
+                    }
                     store4<K>(dk + q + off, key);
                     *reinterpret_cast<uint4*>(dg + q + off) = make_uint4(g[0], g[1], g[2], g[3]);
 #pragma unroll
@@ -689,7 +700,26 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                             load4<K>(dk + qn + off, kn);
                             gn = *reinterpret_cast<const uint4*>(dg + qn + off);
                         }
-                        place(k4[0], g4.x); place(k4[1], g4.y); place(k4[2], g4.z); place(k4[3], g4.w);
+                        {
+                            const uint32_t gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                            uint32_t bb[4];
+                            bool in[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                bb[k] = (uint32_t)((k4[k] - kmin) >> shift);
+                                in[k] = gg[k] != kInvalid && bb[k] >= blo && bb[k] < bhi;
+                            }
+                            uint32_t pos[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                if (in[k]) pos[k] = atomicAdd(&hall[bb[k]], 1u) - base;
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                if (!in[k]) continue;
+                                if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = gg[k]; }
+                                else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = gg[k]; }
+                            }
+                        }
                         if (!more) break;
                         q = qn;
                         g4 = gn;
