@@ -294,7 +294,7 @@ int configure_rank(hpdex_plan* p) {
     if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
     const size_t left = budget - L.total;
     int cap = (int)std::min<size_t>(left / (kb + 5), (size_t)1 << 30);  // + big-list entry share
-    cap = std::max(0, cap - 8);
+    cap = std::max(0, cap - 8) & ~7;
     L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
     p->rank_smem = L.total;
 
@@ -303,8 +303,8 @@ int configure_rank(hpdex_plan* p) {
     if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM (smem %zu)", p->rank_smem);
     p->rank_grid = m->dev.sms * blocks;
 
-    // multiple of 8 elements: every CTA's slice starts 32-byte aligned for vector access
-    const long long slice = (m->max_col_nnz + 8 + 7) & ~7ll;
+    // whole 128-byte lines per CTA slice (vector access, bulk copies, L2 discards)
+    const long long slice = rank_slice(m->max_col_nnz);
     const size_t nctas = (size_t)p->rank_grid;
     TRY(p->dk.alloc(nctas * slice * kb));
     TRY(p->dg.alloc(nctas * slice));
@@ -473,7 +473,7 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
 }
 
 int check_device_errors(hpdex_plan* p) {
-    unsigned long long e[2];
+    unsigned long long e[kErrWords];
     CUDA_TRY(cudaMemcpy(e, p->err.p, sizeof e, cudaMemcpyDeviceToHost));
     const unsigned long long G = (unsigned long long)p->G;
     if (e[0] != ~0ull) {
@@ -619,7 +619,7 @@ int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_target
     TRY(p->order.alloc(std::max<long long>(C, 1)));
     if (C) CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
     TRY(p->queue.alloc(1));
-    TRY(p->err.alloc(2));
+    TRY(p->err.alloc(kErrWords));
     const size_t n = (size_t)(p->T * C);
     TRY(p->U1.alloc(std::max<size_t>(n, 1)));
     TRY(p->P.alloc(std::max<size_t>(n, 1)));
@@ -652,7 +652,7 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
             // event-record nodes (a plain record under capture only adds a dependency)
             const unsigned ext = cudaEventRecordExternal;
             if (cudaEventRecordWithFlags(p->ev[0], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
-            if (st == HPDEX_OK && cudaMemsetAsync(p->err.p, 0xff, 2 * sizeof(unsigned long long), s) != cudaSuccess)
+            if (st == HPDEX_OK && cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), s) != cudaSuccess)
                 st = fail(HPDEX_ERR_CUDA, "memset failed");
             if (st == HPDEX_OK) st = enqueue_rank(p, mode, s, &l);
             if (st == HPDEX_OK && cudaEventRecordWithFlags(p->ev[1], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
@@ -669,7 +669,7 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
         launches = (p->m->n_cols > 0 ? 1 : 0) + (p->T * p->m->n_cols > 0 ? 1 : 0);
     } else {
         CUDA_TRY(cudaEventRecord(p->ev[0], s));
-        CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, 2 * sizeof(unsigned long long), s));
+        CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), s));
         TRY(enqueue_rank(p, mode, s, &launches));
         CUDA_TRY(cudaEventRecord(p->ev[1], s));
         if (exact) {
@@ -901,7 +901,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     size_t off = 0;
     auto take = [&](size_t bytes) { unsigned char* p = base + off; off = RankSmem::align16(off + bytes); return p; };
     int32_t* queue = reinterpret_cast<int32_t*>(take(sizeof(int32_t)));
-    unsigned long long* err = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
+    unsigned long long* err = reinterpret_cast<unsigned long long*>(take(kErrWords * sizeof(unsigned long long)));
     unsigned long long* max_col = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
     long long* group_rows = reinterpret_cast<long long*>(take(sizeof(long long) * G));
     const size_t header_bytes = off;
@@ -922,7 +922,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     // every call shares the array and finds the previous call's contents: clear what
     // must start at zero (work counter, group sizes, longest column) and reset the error words
     CUDA_TRY(cudaMemsetAsync(base, 0, header_bytes, s));
-    CUDA_TRY(cudaMemsetAsync(err, 0xff, 2 * sizeof(unsigned long long), s));
+    CUDA_TRY(cudaMemsetAsync(err, 0xff, kErrWords * sizeof(unsigned long long), s));
     if (C == 0) return HPDEX_OK;
     {
         const int grid = (int)std::min<long long>(std::max<long long>((std::max<long long>((long long)n_rows, C) + 255) / 256, 1),
@@ -950,7 +950,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     RankSmem L(nbl, G, tie_warps, 1, 1, 0, kb);
     if (L.total + 16384 > budget) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: layout does not fit");
     int cap = (int)std::min<size_t>((budget - L.total) / (kb + 5), (size_t)1 << 30);
-    cap = std::max(0, cap - 8);
+    cap = std::max(0, cap - 8) & ~7;
     L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
     int blocks = 0;
     TRY(rank_status(rank_occupancy(dtype, L.total, nd->info.smem_optin, 1, &blocks), "rank kernel set-up"));
@@ -963,12 +963,13 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     // per CTA: a decoded copy of the current column and, for columns larger than the
     // shared-memory capacity, a bucket-ordered slab slice
     const int nslices = (long long)longest > cap ? 2 : 1;
+    off = (off + 127) & ~(size_t)127;  // slices in whole 128-byte lines
     const size_t left = off + 512 * (size_t)grid < kNoAllocScratchBytes ? kNoAllocScratchBytes - off - 512 * (size_t)grid : 0;
-    const long long slice = (long long)(left / ((size_t)grid * nslices * (kb + 4))) & ~7ll;
-    if ((long long)longest + 8 > slice)
+    const long long slice = (long long)(left / ((size_t)grid * nslices * (kb + 4))) & ~31ll;
+    if (rank_slice((long long)longest) > slice)
         return fail(HPDEX_ERR_UNSUPPORTED,
                     "hpdex_mannwhitneyu_noalloc: a column holds %llu entries, above the %lld the "
-                    "fixed scratch allows at this size", longest, slice - 8);
+                    "fixed scratch allows at this size", longest, slice - 71);
     void* dk = take((size_t)grid * slice * kb);
     uint32_t* dg = reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4));
     void* ek = nslices == 2 ? take((size_t)grid * slice * kb) : nullptr;
@@ -1025,7 +1026,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     mwu_pvalue_asymptotic_kernel<<<(int)std::min<long long>((pa.n + 255) / 256, (long long)nd->info.sms * 8), 256, 0, s>>>(pa);
     CUDA_TRY(cudaGetLastError());
 
-    unsigned long long e[2];
+    unsigned long long e[kErrWords];
     CUDA_TRY(cudaMemcpyAsync(e, err, sizeof e, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     const unsigned long long Gu = (unsigned long long)G;

@@ -11,23 +11,30 @@
 // slice for every target: reference ranks come from one bucket index per gene.
 //
 // Per gene:
-//   pass 1  (HBM) 4-wide vector loads of row ids and values, group id gather, decode to
-//           (key, group) written at the entry's position in the CTA's scratch slice;
-//           value-bucket histograms of all stored elements and of reference elements
-//           (bucket = top bits of key - column minimum key, from the resident matrix's column
-//           key ranges); per-group stored counts (and negatives for zero_handling=mix)
+//   pass 1  (HBM, evict-first loads) 4-wide vector loads of row ids and values, group id
+//           gathers, decode to (key, group) written at the entry's position in the CTA's
+//           scratch slice; value-bucket histograms of all stored elements and of reference
+//           elements (bucket = top bits of key - column minimum key, from the resident
+//           matrix's column key ranges); per-group stored counts (negatives for mix)
 //   scan    exclusive prefix sums -> bucket start, reference count below each bucket
-//   slabs   consecutive bucket ranges holding at most the shared-memory element capacity;
-//           per slab:
+//   slabs   the whole gene when it fits in shared memory, else consecutive bucket ranges
+//           holding at most the shared-memory element capacity; per slab:
 //   pass 2  (L2) scatter the slab's decoded elements into bucket order in shared memory (a
-//           slab made of one bucket larger than half the capacity uses a global slice)
+//           slab made of one bucket larger than half the capacity uses a global slice);
+//           after the last slab the decoded copy is dropped from L2 without write-back
+//           (discard.global.L2)
 //   rank    32-bucket chunks to all warps: singleton buckets add one term; buckets of 2..8
-//           elements are resolved four at a time per warp, 9..32 one per warp, both with
-//           warp match instructions (equal keys, equal (key, group)); larger buckets go to a
-//           list that warps drain one bucket at a time with per-warp group counters: one
+//           elements are resolved four at a time per warp, 9..32 one per warp: reference
+//           lanes are broadcast to count smaller / equal reference keys, per-warp group
+//           counters find repeated (key, group) pairs; larger buckets go to a list that
+//           warps drain one bucket at a time with per-warp group counters: one
 //           representative per (run of equal keys, target) adds s*(2*lref + c0) to A and
 //           (c0+s)^3-(c0+s)-(c0^3-c0) to B
 //   final   zero block, U1, tie sum per target
+//
+// Shared-memory accumulators use 32-bit atomics (a 64-bit value is updated as two halves
+// with an explicit carry): on sm_103a a 64-bit shared atomic add costs about five times a
+// 32-bit one, and warp match instructions about six ballots, so neither is used per round.
 //
 // "Stored" elements are what the reference gathers into its slices (mannwhitneyu.cpp:
 // 914-926): row id in [0, n_rows), group in [0, G), finite value; for zero_handling
@@ -40,6 +47,8 @@
 #include "common.cuh"
 
 namespace hpdex {
+
+constexpr int kErrWords = 2;  // error words of a run, reset to all ones before it
 
 struct RankArgs {
     const void* data;          // values of the CSC matrix (dtype V)
@@ -70,7 +79,7 @@ struct RankArgs {
     uint32_t* dg_global;       // decoded groups (kInvalid: not stored)
     void* ek_global;           // bucket-ordered elements of a slab too big for shared memory
     uint32_t* eg_global;
-    long long slice;           // >= longest column + 4, multiple of 8
+    long long slice;           // rank_slice(longest column): multiple of 32 elements
     unsigned char* acc_global; // per CTA 24*G bytes when the accumulators are not in SMEM
     uint32_t* cnt_global;      // per CTA and warp: packed counters (when not in SMEM), then
                                // G 32-bit counters (buckets of more than 65535 elements)
@@ -85,6 +94,12 @@ constexpr int kSmallBucket = 8;    // 2..8: four buckets per warp round
 constexpr int kMediumBucket = 32;  // 9..32: one warp round
 constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum per bucket
 constexpr uint32_t kInvalid = 0xffffffffu;
+// Scratch slice per CTA: the longest column plus the 4-entry alignment offset, in whole
+// 128-byte lines of 32-bit elements (discard.global.L2 works on lines, so no line of a
+// slice is shared with another CTA's slice).
+__host__ __device__ inline long long rank_slice(long long longest) {
+    return (longest + 40 + 31) & ~31ll;
+}
 
 // Shared-memory layout shared by host (sizing) and device (carving): bucket starts and
 // reference counts (NB + 1 each), the slab's list of large buckets, accumulators, run
@@ -106,6 +121,66 @@ struct RankSmem {
         total = hist_bytes + acc_bytes + cnt_bytes + elem_bytes;
     }
 };
+
+// ---------------------------------------------------------------------------------------
+// Atomics. SH = the address is in shared memory: explicit .shared forms, so that a pointer
+// that reaches a helper as a generic pointer still compiles to a shared-memory atomic.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+template <bool SH>
+__device__ __forceinline__ void red_add(uint32_t* p, uint32_t v) {
+    if constexpr (SH) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+    else atomicAdd(p, v);
+}
+template <bool SH>
+__device__ __forceinline__ uint32_t atom_add(uint32_t* p, uint32_t v) {
+    if constexpr (SH) {
+        uint32_t o;
+        asm volatile("atom.shared.add.u32 %0, [%1], %2;" : "=r"(o) : "r"(smem_addr(p)), "r"(v) : "memory");
+        return o;
+    } else {
+        return atomicAdd(p, v);
+    }
+}
+template <bool SH>
+__device__ __forceinline__ uint32_t atom_and(uint32_t* p, uint32_t v) {
+    if constexpr (SH) {
+        uint32_t o;
+        asm volatile("atom.shared.and.b32 %0, [%1], %2;" : "=r"(o) : "r"(smem_addr(p)), "r"(v) : "memory");
+        return o;
+    } else {
+        return atomicAnd(p, v);
+    }
+}
+// 64-bit accumulator update: in shared memory a 32-bit add to the low half whose wrap-around
+// (seen in the value the atomic returns) carries into the high half; the halves are only
+// read as one 64-bit value after a block barrier. Global memory: native 64-bit atomics.
+template <bool SH>
+__device__ __forceinline__ void acc_add(unsigned long long* p, unsigned long long v) {
+    if constexpr (SH) {
+        uint32_t* w = reinterpret_cast<uint32_t*>(p);
+        const uint32_t lo = (uint32_t)v;
+        uint32_t hi = (uint32_t)(v >> 32);
+        if (lo) {
+            const uint32_t old = atom_add<true>(w, lo);
+            hi += (uint32_t)(old + lo < old);
+        }
+        if (hi) red_add<true>(w + 1, hi);
+    } else {
+        if (v) atomicAdd(p, v);
+    }
+}
+
+// Drops the 128-byte L2 lines of [p, p + bytes) without write-back (p 128-byte aligned; the
+// lines belong to this CTA's scratch slice and hold nothing that is read again).
+template <int NT>
+__device__ __forceinline__ void l2_discard(const void* p, size_t bytes) {
+    const char* b = static_cast<const char*>(p);
+    for (size_t o = (size_t)threadIdx.x * 128; o < bytes; o += (size_t)NT * 128)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(b + o) : "memory");
+}
 
 template <int NT>
 __device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint32_t* wsy,
@@ -139,26 +214,29 @@ __device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint
     __syncthreads();
 }
 
+// Streaming (evict-first) loads of the matrix: each entry is read once per run.
+__device__ __forceinline__ int4 ld_stream(const int4* p) { return __ldcs(p); }
 // 4 consecutive values starting at a 4-element-aligned position, one or two vector loads
-template <class V>
+template <class V, bool STREAM>
 __device__ __forceinline__ void load4(const V* p, V (&v)[4]) {
     if constexpr (sizeof(V) == 4) {
-        const uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+        const uint4 u = STREAM ? __ldcs(reinterpret_cast<const uint4*>(p)) : *reinterpret_cast<const uint4*>(p);
         v[0] = __builtin_bit_cast(V, u.x); v[1] = __builtin_bit_cast(V, u.y);
         v[2] = __builtin_bit_cast(V, u.z); v[3] = __builtin_bit_cast(V, u.w);
     } else if constexpr (sizeof(V) == 8) {
-        const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(p));
-        const ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(p) + 1);
+        const ulonglong2* q = reinterpret_cast<const ulonglong2*>(p);
+        const ulonglong2 a = STREAM ? __ldcs(q) : q[0];
+        const ulonglong2 b = STREAM ? __ldcs(q + 1) : q[1];
         v[0] = __builtin_bit_cast(V, a.x); v[1] = __builtin_bit_cast(V, a.y);
         v[2] = __builtin_bit_cast(V, b.x); v[3] = __builtin_bit_cast(V, b.y);
     } else if constexpr (sizeof(V) == 2) {
-        const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+        const uint2 u = STREAM ? __ldcs(reinterpret_cast<const uint2*>(p)) : *reinterpret_cast<const uint2*>(p);
         v[0] = __builtin_bit_cast(V, (uint16_t)(u.x & 0xffffu));
         v[1] = __builtin_bit_cast(V, (uint16_t)(u.x >> 16));
         v[2] = __builtin_bit_cast(V, (uint16_t)(u.y & 0xffffu));
         v[3] = __builtin_bit_cast(V, (uint16_t)(u.y >> 16));
     } else {
-        const uint32_t u = __ldg(reinterpret_cast<const uint32_t*>(p));
+        const uint32_t u = STREAM ? __ldcs(reinterpret_cast<const unsigned int*>(p)) : *reinterpret_cast<const uint32_t*>(p);
         v[0] = __builtin_bit_cast(V, (uint8_t)(u & 0xffu));
         v[1] = __builtin_bit_cast(V, (uint8_t)((u >> 8) & 0xffu));
         v[2] = __builtin_bit_cast(V, (uint8_t)((u >> 16) & 0xffu));
@@ -180,12 +258,14 @@ __device__ __forceinline__ void store4(K* p, const K (&k)[4]) {
 // Per-warp, per-group counters of a run, 16 bits each (two groups per 32-bit word). A run
 // never counts more than 65535 elements of one group here: buckets with more than 65535
 // elements are resolved with 32-bit counters instead.
+template <bool SH>
 __device__ __forceinline__ void cnt_inc(uint32_t* cnt, uint32_t g) {
-    atomicAdd(&cnt[g >> 1], (g & 1u) ? 0x10000u : 1u);
+    red_add<SH>(&cnt[g >> 1], (g & 1u) ? 0x10000u : 1u);
 }
+template <bool SH>
 __device__ __forceinline__ uint32_t cnt_take(uint32_t* cnt, uint32_t g) {
     // returns the count and clears it; only the first caller per group sees it nonzero
-    const uint32_t old = atomicAnd(&cnt[g >> 1], (g & 1u) ? 0x0000ffffu : 0xffff0000u);
+    const uint32_t old = atom_and<SH>(&cnt[g >> 1], (g & 1u) ? 0x0000ffffu : 0xffff0000u);
     return (g & 1u) ? (old >> 16) : (old & 0xffffu);
 }
 __device__ __forceinline__ void cntw_inc(uint32_t* cnt, uint32_t g) { atomicAdd(&cnt[g], 1u); }
@@ -216,50 +296,70 @@ struct Acc {
 
 // Adds the contribution of s equal (key, target g) elements whose run has c0 reference
 // elements and lref reference elements below it.
+template <bool SH>
 __device__ __forceinline__ void add_pair(const Acc& acc, uint32_t g, unsigned long long s,
                                          unsigned long long lref, unsigned long long c0) {
-    atomicAdd(&acc.A[g], s * (2ull * lref + c0));
-    const unsigned long long tb = tie_delta(c0, s);
-    if (tb) atomicAdd(&acc.B[g], tb);
+    acc_add<SH>(&acc.A[g], s * (2ull * lref + c0));
+    acc_add<SH>(&acc.B[g], tie_delta(c0, s));
 }
 
 // One warp round over up to 32 elements of buckets that lie wholly inside the round:
 // lane L holds (key, g) when active; `sub` is the lane mask of L's bucket, rb its reference
-// count below. Equal keys and equal (key, group) come from warp match instructions; the
-// lowest lane of each (key, group) set adds the set's contribution.
-template <class K>
+// count below. Every element adds its own share, so no representative is needed:
+//   target: A += 2*(rb + lt) + c0, B += 3c0^2 + 3c0*s + s^2 - 1
+//   reference: T_ref += c0^2 - 1
+// where lt / c0 count the reference elements of the bucket with a smaller / equal key and s
+// the target elements with the same key and group. Summed over a run of c0 reference and
+// s target-g elements these give s*(2*lref + c0), (c0+s)^3-(c0+s)-(c0^3-c0) and c0^3-c0.
+// lt and c0 come from broadcasting the (few) reference lanes; s from the warp's group
+// counters, which show which groups occur more than once in the round, and a pairwise
+// comparison among those lanes only. `cnt` is zero on entry and on exit.
+template <class K, bool SH>
 __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, unsigned sub,
-                                              uint32_t rb, const Acc& acc,
+                                              uint32_t rb, const Acc& acc, uint32_t* cnt,
                                               unsigned long long& tref) {
-    const int lane = threadIdx.x & 31;
     const unsigned act = __ballot_sync(0xffffffffu, active);
     if (!act) return;
-    const unsigned refm = __ballot_sync(0xffffffffu, active && g == 0u);
-    if (active) {
-        const unsigned mk = __match_any_sync(act, key) & sub;  // same key, same bucket
-        const unsigned mg = __match_any_sync(act, g);
-        const unsigned pair = mk & mg;
-        const uint32_t c0 = __popc(mk & refm);
-        const bool leader_key = (__ffs((int)mk) - 1) == lane;
-        // reference elements of my bucket with a smaller key: sum over the other keys'
-        // leaders (few: one per distinct key)
-        uint32_t lt = 0;
-        unsigned leaders = __ballot_sync(act, leader_key);
-        const bool impure_any = __any_sync(act, mk != (sub & act));
-        if (impure_any) {
-            while (leaders) {
-                const int j = __ffs((int)leaders) - 1;
-                leaders &= leaders - 1u;
-                const K kj = __shfl_sync(act, key, j);
-                const uint32_t cj = __shfl_sync(act, c0, j);
-                if (((sub >> j) & 1u) && kj < key) lt += cj;
-            }
+    const bool is_ref = active && g == 0u;
+    const bool is_tar = active && g != 0u;
+    const unsigned refm = __ballot_sync(0xffffffffu, is_ref);
+    uint32_t lt = 0, c0 = 0;
+    for (unsigned r = refm; r; r &= r - 1u) {
+        const int j = __ffs((int)r) - 1;
+        const K kj = __shfl_sync(0xffffffffu, key, j);
+        if ((sub >> j) & 1u) {
+            lt += kj < key;
+            c0 += kj == key;
         }
-        if ((__ffs((int)pair) - 1) == lane) {
-            const uint32_t s = __popc(pair);
-            if (g) add_pair(acc, g, s, (unsigned long long)rb + lt, c0);
-            else tref += (unsigned long long)c0 * c0 * c0 - c0;  // s == c0 for the reference
+    }
+    if (is_tar) cnt_inc<SH>(cnt, g);
+    __syncwarp();
+    uint32_t ng = 0;
+    if (is_tar) {
+        const uint32_t w = cnt[g >> 1];
+        ng = (g & 1u) ? (w >> 16) : (w & 0xffffu);
+    }
+    __syncwarp();
+    if (is_tar) cnt[g >> 1] = 0u;  // clears both groups of the word; both were read above
+    const unsigned rep = __ballot_sync(0xffffffffu, ng > 1u);
+    uint32_t s = 1;
+    if (rep) {
+        uint32_t c = 0;
+        for (unsigned r = rep; r; r &= r - 1u) {
+            const int j = __ffs((int)r) - 1;
+            const K kj = __shfl_sync(0xffffffffu, key, j);
+            const uint32_t gj = __shfl_sync(0xffffffffu, g, j);
+            c += (gj == g && kj == key);
         }
+        if (ng > 1u) s = c;
+    }
+    __syncwarp();
+    if (is_tar) {
+        acc_add<SH>(&acc.A[g], 2ull * ((unsigned long long)rb + lt) + c0);
+        const uint32_t tb = 3u * c0 * c0 + 3u * c0 * s + s * s - 1u;  // c0, s <= 32
+        if (tb) acc_add<SH>(&acc.B[g], tb);
+    } else if (is_ref) {
+        tref += (unsigned long long)c0 * c0 - 1ull;
     }
 }
 
@@ -269,10 +369,19 @@ __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, un
 // per group adds the contribution). Impure buckets undo the counts and visit their distinct
 // keys in ascending order (warp minimum), two passes per key; after kMaxRunsByMin keys the
 // rest is resolved element by element. Counters are zero on entry and on exit.
-template <class K, bool WIDE, class EK, class EG>
+// SH: accumulators in shared memory; SHC: counters in shared memory.
+template <class K, bool WIDE, bool SH, bool SHC, class EK, class EG>
 __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, const EG* eg,
                             const Acc& acc, uint32_t* cnt, unsigned long long& tref) {
     const int lane = threadIdx.x & 31;
+    auto inc = [&](uint32_t g) {
+        if constexpr (WIDE) cntw_inc(cnt, g);
+        else cnt_inc<SHC>(cnt, g);
+    };
+    auto take = [&](uint32_t g) -> uint32_t {
+        if constexpr (WIDE) return cntw_take(cnt, g);
+        else return cnt_take<SHC>(cnt, g);
+    };
     K lo = ~K(0), hi = K(0);
     uint32_t c0 = 0;
     for (uint32_t j = lane; j < m; j += 32) {
@@ -280,11 +389,8 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
         const uint32_t g = eg[s0 + j];
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
-        if (g) {
-            if (WIDE) cntw_inc(cnt, g); else cnt_inc(cnt, g);
-        } else {
-            ++c0;
-        }
+        if (g) inc(g);
+        else ++c0;
     }
     lo = wmin<K>(0xffffffffu, lo);
     hi = wmax<K>(0xffffffffu, hi);
@@ -294,8 +400,8 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
         for (uint32_t j = lane; j < m; j += 32) {
             const uint32_t g = eg[s0 + j];
             if (g) {
-                const uint32_t s = WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g);
-                if (s) add_pair(acc, g, s, rb, c0);
+                const uint32_t s = take(g);
+                if (s) add_pair<SH>(acc, g, s, rb, c0);
             }
         }
         if (lane == 0) tref += (unsigned long long)c0 * c0 * c0 - c0;
@@ -305,7 +411,7 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
     // impure: clear the counts, then one key at a time
     for (uint32_t j = lane; j < m; j += 32) {
         const uint32_t g = eg[s0 + j];
-        if (g) (void)(WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g));
+        if (g) (void)take(g);
     }
     __syncwarp();
     unsigned long long lref = rb;
@@ -315,11 +421,8 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
         for (uint32_t j = lane; j < m; j += 32) {
             if (ek[s0 + j] != cur) continue;
             const uint32_t g = eg[s0 + j];
-            if (g) {
-                if (WIDE) cntw_inc(cnt, g); else cnt_inc(cnt, g);
-            } else {
-                ++r0;
-            }
+            if (g) inc(g);
+            else ++r0;
         }
         r0 = __reduce_add_sync(0xffffffffu, r0);
         __syncwarp();
@@ -330,8 +433,8 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
             if (k == cur) {
                 const uint32_t g = eg[s0 + j];
                 if (g) {
-                    const uint32_t s = WIDE ? cntw_take(cnt, g) : cnt_take(cnt, g);
-                    if (s) add_pair(acc, g, s, lref, r0);
+                    const uint32_t s = take(g);
+                    if (s) add_pair<SH>(acc, g, s, lref, r0);
                 }
             } else if (k > cur) {
                 nxt = k < nxt ? k : nxt;
@@ -359,10 +462,9 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
                     sc += (gj == g && kj == k);
                 }
                 if (g) {
-                    atomicAdd(&acc.A[g], 2ull * (lref + lt) + e0);
+                    acc_add<SH>(&acc.A[g], 2ull * (lref + lt) + e0);
                     const unsigned long long cc = e0, ss = sc;
-                    const unsigned long long tb = 3ull * cc * cc + 3ull * cc * ss + ss * ss - 1ull;
-                    if (tb) atomicAdd(&acc.B[g], tb);
+                    acc_add<SH>(&acc.B[g], 3ull * cc * cc + 3ull * cc * ss + ss * ss - 1ull);
                 } else {
                     tref += (unsigned long long)e0 * e0 - 1ull;
                 }
@@ -375,8 +477,8 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
 }
 
 // Rank phase of one slab: elements [0, cnt) in bucket order in ek/eg, buckets [blo, bhi)
-// starting at `base` in the gene's bucket order.
-template <class K, class EK, class EG>
+// starting at `base` in the gene's bucket order (hall[b - 1] = start of bucket b).
+template <class K, bool SH, class EK, class EG>
 __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi, uint32_t base,
                           const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
@@ -399,7 +501,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
         const uint32_t s0 = sb - base;
         if (m == 1u) {
             const uint32_t g = eg[s0];
-            if (g) atomicAdd(&acc.A[g], 2ull * rb);  // a lone target value: no reference tie
+            if (g) acc_add<SH>(&acc.A[g], 2ull * rb);  // a lone target value: no reference tie
         }
         bool spill = false;
         if (m > (uint32_t)kMediumBucket) {
@@ -425,7 +527,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             K key = K(0);
             uint32_t g = 0;
             if (active) { key = ek[sq + e]; g = eg[sq + e]; }
-            resolve_round<K>(active, key, g, 0xffu << (8 * q), rq, acc, tref);
+            resolve_round<K, SH>(active, key, g, 0xffu << (8 * q), rq, acc, cnt, tref);
         }
         // buckets of 9..32 elements: one round each
         unsigned mmask = __ballot_sync(0xffffffffu, m > (uint32_t)kSmallBucket && m <= (uint32_t)kMediumBucket);
@@ -439,7 +541,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             K key = K(0);
             uint32_t g = 0;
             if (active) { key = ek[sj + lane]; g = eg[sj + lane]; }
-            resolve_round<K>(active, key, g, 0xffffffffu, rj, acc, tref);
+            resolve_round<K, SH>(active, key, g, 0xffffffffu, rj, acc, cnt, tref);
         }
         unsigned over = __ballot_sync(0xffffffffu, spill);
         while (over) {
@@ -448,8 +550,8 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             const uint32_t mj = __shfl_sync(0xffffffffu, m, j);
             const uint32_t sj = __shfl_sync(0xffffffffu, s0, j);
             const uint32_t rj = __shfl_sync(0xffffffffu, rb, j);
-            if (mj <= 65535u) resolve_big<K, false>(sj, mj, rj, ek, eg, acc, cnt, tref);
-            else resolve_big<K, true>(sj, mj, rj, ek, eg, acc, wide_cnt, tref);
+            if (mj <= 65535u) resolve_big<K, false, SH, SH>(sj, mj, rj, ek, eg, acc, cnt, tref);
+            else resolve_big<K, true, SH, false>(sj, mj, rj, ek, eg, acc, wide_cnt, tref);
         }
     }
     __syncthreads();
@@ -462,8 +564,8 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
         const uint32_t b = biglist[q];
         const uint32_t sb = (b == blo) ? base : hall[b - 1];
         const uint32_t m = hall[b] - sb;
-        if (m <= 65535u) resolve_big<K, false>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
-        else resolve_big<K, true>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
+        if (m <= 65535u) resolve_big<K, false, SH, SH>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
+        else resolve_big<K, true, SH, false>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
     }
 }
 
@@ -517,7 +619,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
     for (int i = tid; i < a.tie_warps * G; i += NT) wide_base[i] = 0u;
-    if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
+    if (tid == 0) {
+        s_chunk = 0u; s_nbig = 0u; s_bigi = 0u;
+    }
 
     bool first = true;
     for (;;) {
@@ -568,27 +672,27 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
-        auto decode = [&](int32_t r, V v, K& key) -> uint32_t {
-            if ((uint32_t)r >= nrows) return kInvalid;  // negative ids wrap above n_rows
-            const int g = __ldg(gidp + r);
-            if ((unsigned)g >= (unsigned)G) return kInvalid;
-            if (!Val<V>::finite(v)) return kInvalid;
-            if (zh != ZH_NONE && Val<V>::zero(v)) return kInvalid;
-            key = Val<V>::key(v);
-            return (uint32_t)g;
-        };
         auto count = [&](uint32_t g, K key, V v) {
-            if (g) atomicAdd(&nz[g], 1u);
+            if (g) red_add<ACC_SMEM>(&nz[g], 1u);
             else ++nref_local;
-            if (zh == ZH_MIX && Val<V>::neg(v)) atomicAdd(&ng[g], 1u);
+            if (zh == ZH_MIX && Val<V>::neg(v)) red_add<ACC_SMEM>(&ng[g], 1u);
             const uint32_t b = (uint32_t)((key - kmin) >> shift);
-            atomicAdd(&hall[b], 1u);
-            if (g == 0) atomicAdd(&href[b], 1u);
+            red_add<true>(&hall[b], 1u);
+            if (g == 0) red_add<true>(&href[b], 1u);
         };
         auto scalar1 = [&](uint32_t i) {
-            K key = K(0);
+            const int32_t r = rows[i];
             const V v = data[i];
-            const uint32_t g = decode(rows[i], v, key);
+            uint32_t g = kInvalid;
+            K key = K(0);
+            if ((uint32_t)r < nrows) {  // negative ids wrap above n_rows
+                const int gr = __ldg(gidp + r);
+                if ((unsigned)gr < (unsigned)G && Val<V>::finite(v) &&
+                    (zh == ZH_NONE || !Val<V>::zero(v))) {
+                    g = (uint32_t)gr;
+                    key = Val<V>::key(v);
+                }
+            }
             dk[i + off] = key;
             dg[i + off] = g;
             if (g != kInvalid) count(g, key, v);
@@ -597,17 +701,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         {
             uint32_t q = ia + 4u * tid;
             if (q < ib) {
-                int4 r = __ldg(reinterpret_cast<const int4*>(rows + q));
+                int4 r = ld_stream(reinterpret_cast<const int4*>(rows + q));
                 V v[4];
-                load4<V>(data + q, v);
+                load4<V, true>(data + q, v);
                 for (;;) {
                     const uint32_t qn = q + 4u * NT;
                     const bool more = qn < ib;
                     int4 rn = make_int4(-1, -1, -1, -1);
                     V vn[4] = {V(0), V(0), V(0), V(0)};
                     if (more) {
-                        rn = __ldg(reinterpret_cast<const int4*>(rows + qn));
-                        load4<V>(data + qn, vn);
+                        rn = ld_stream(reinterpret_cast<const int4*>(rows + qn));
+                        load4<V, true>(data + qn, vn);
                     }
                     const int32_t rr[4] = {r.x, r.y, r.z, r.w};
                     // all four group-id gathers in flight before any of them is tested
@@ -640,23 +744,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         }
         for (uint32_t i = ib + tid; i < nraw; i += NT) scalar1(i);
         nref_local = __reduce_add_sync(0xffffffffu, nref_local);
-        if (lane == 0 && nref_local) atomicAdd(&nz[0], nref_local);
+        if (lane == 0 && nref_local) red_add<ACC_SMEM>(&nz[0], nref_local);
         __syncthreads();
         block_scan2<NT>(hall, href, NB, s_wsx, s_wsy, &s_maxb);
         const uint32_t n = hall[NB];
         const uint32_t cap = (uint32_t)a.elem_smem_cap;
-        // slabs: buckets whose start offset lies in [k*W, (k+1)*W) form slab k; a slab holds
-        // at most W + (largest bucket) elements, which fits the shared-memory capacity unless a
-        // single bucket is larger than half of it (then that slab uses the global slice)
+        // slabs: the whole gene when it fits in shared memory; else buckets whose start lies
+        // in [k*W, (k+1)*W) form slab k, which holds at most W + (largest bucket) elements:
+        // that fits the capacity unless one bucket is larger than half of it (such a slab is
+        // placed in the global slice)
         const uint32_t maxb = s_maxb;
-        uint32_t W;
-        if (cap < 1024u) {
-            W = max(n, 1u);  // (almost) no shared memory for elements: one slab, global slice
-        } else {
-            W = cap > maxb ? cap - maxb : 0u;
-            W = max(W, cap / 2u);
+        uint32_t W = n, nslabs = n ? 1u : 0u;
+        if (n > cap && cap >= 1024u) {
+            W = max(cap > maxb ? cap - maxb : 0u, cap / 2u);
+            nslabs = (n - 1u) / W + 1u;
         }
-        const uint32_t nslabs = n ? (n - 1u) / W + 1u : 0u;
 
         // During a slab's scatter hall[b] counts up from the start to the end of bucket b,
         // so afterwards the start of bucket b is hall[b - 1] (or the slab base for its first
@@ -665,10 +767,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         uint32_t blo = 0;
         for (uint32_t slab = 0; slab < nslabs; ++slab) {
             if (tid == 0) {
-                uint32_t lo = blo, hi = (uint32_t)NB;
-                const uint32_t t1 = (slab + 1u) * W;
-                while (lo < hi) { const uint32_t mid = (lo + hi) >> 1; if (hall[mid] < t1) lo = mid + 1; else hi = mid; }
-                s_slab_hi = (slab + 1u == nslabs) ? (uint32_t)NB : lo;
+                uint32_t bh = (uint32_t)NB;
+                if (slab + 1u < nslabs) {  // first b >= blo whose start is >= (slab + 1) * W
+                    uint32_t lo = blo, hi = (uint32_t)NB;
+                    const uint32_t t1 = (slab + 1u) * W;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (hall[mid] < t1) lo = mid + 1u; else hi = mid;
+                    }
+                    bh = lo;
+                }
+                s_slab_hi = bh;
             }
             __syncthreads();
             const uint32_t bhi = s_slab_hi;
@@ -677,11 +786,12 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
             // ---- pass 2 (L2): scatter this slab's decoded elements into bucket order ----
             if (cnt_slab) {
+                const bool all = nslabs == 1u;
                 auto place = [&](K key, uint32_t g) {
                     if (g == kInvalid) return;
                     const uint32_t b = (uint32_t)((key - kmin) >> shift);
-                    if (b < blo || b >= bhi) return;
-                    const uint32_t pos = atomicAdd(&hall[b], 1u) - base;
+                    if (!all && (b < blo || b >= bhi)) return;
+                    const uint32_t pos = atom_add<true>(&hall[b], 1u) - base;
                     if (in_smem) { ek_s[pos] = key; eg_s[pos] = g; }
                     else { ek_g[pos] = key; eg_g[pos] = g; }
                 };
@@ -689,7 +799,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 uint32_t q = ia + 4u * tid;
                 if (q < ib) {
                     K k4[4];
-                    load4<K>(dk + q + off, k4);
+                    load4<K, false>(dk + q + off, k4);
                     uint4 g4 = *reinterpret_cast<const uint4*>(dg + q + off);
                     for (;;) {
                         const uint32_t qn = q + 4u * NT;
@@ -697,28 +807,26 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                         K kn[4] = {K(0), K(0), K(0), K(0)};
                         uint4 gn = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
                         if (more) {
-                            load4<K>(dk + qn + off, kn);
+                            load4<K, false>(dk + qn + off, kn);
                             gn = *reinterpret_cast<const uint4*>(dg + qn + off);
                         }
-                        {
-                            const uint32_t gg[4] = {g4.x, g4.y, g4.z, g4.w};
-                            uint32_t bb[4];
-                            bool in[4];
+                        const uint32_t gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                        uint32_t bb[4];
+                        bool in[4];
 #pragma unroll
-                            for (int k = 0; k < 4; ++k) {
-                                bb[k] = (uint32_t)((k4[k] - kmin) >> shift);
-                                in[k] = gg[k] != kInvalid && bb[k] >= blo && bb[k] < bhi;
-                            }
-                            uint32_t pos[4];
+                        for (int k = 0; k < 4; ++k) {
+                            bb[k] = (uint32_t)((k4[k] - kmin) >> shift);
+                            in[k] = gg[k] != kInvalid && (all || (bb[k] >= blo && bb[k] < bhi));
+                        }
+                        uint32_t pos[4];
 #pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                if (in[k]) pos[k] = atomicAdd(&hall[bb[k]], 1u) - base;
+                        for (int k = 0; k < 4; ++k)
+                            if (in[k]) pos[k] = atom_add<true>(&hall[bb[k]], 1u) - base;
 #pragma unroll
-                            for (int k = 0; k < 4; ++k) {
-                                if (!in[k]) continue;
-                                if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = gg[k]; }
-                                else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = gg[k]; }
-                            }
+                        for (int k = 0; k < 4; ++k) {
+                            if (!in[k]) continue;
+                            if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = gg[k]; }
+                            else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = gg[k]; }
                         }
                         if (!more) break;
                         q = qn;
@@ -730,14 +838,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 for (uint32_t i = ib + tid; i < nraw; i += NT) place(dk[i + off], dg[i + off]);
             }
             __syncthreads();
+            if (slab + 1u == nslabs) {
+                // the decoded copy is dead: drop its lines from L2 instead of writing them back
+                l2_discard<NT>(dk, (size_t)(nraw + off) * sizeof(K));
+                l2_discard<NT>(dg, (size_t)(nraw + off) * 4u);
+            }
 
             // ---- rank ----
             if (in_smem)
-                rank_slab<K>(ek_s, eg_s, blo, bhi, base, hall, href, biglist, biglist_cap,
-                             &s_chunk, &s_nbig, &s_bigi, acc, cnt, wide_cnt, tref);
+                rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
+                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                       wide_cnt, tref);
             else
-                rank_slab<K>(ek_g, eg_g, blo, bhi, base, hall, href, biglist, biglist_cap,
-                             &s_chunk, &s_nbig, &s_bigi, acc, cnt, wide_cnt, tref);
+                rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
+                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                       wide_cnt, tref);
             __syncthreads();
             if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
             blo = bhi;
