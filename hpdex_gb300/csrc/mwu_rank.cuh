@@ -83,7 +83,8 @@ struct RankArgs {
     unsigned char* acc_global; // per CTA 24*G bytes when the accumulators are not in SMEM
     uint32_t* cnt_global;      // per CTA and warp: packed counters (when not in SMEM), then
                                // G 32-bit counters (buckets of more than 65535 elements)
-    int32_t nb_max_log2;       // bucket table capacity (power of two)
+    int32_t nb_max_log2;       // bucket table capacity (power of two, at most 2^13: the scan
+                               // holds 8 entries per thread)
     int32_t elem_smem_cap;     // elements that fit in shared memory
     int32_t acc_in_smem;       // accumulators and packed run counters in shared memory
     int32_t cnt_in_smem;       // (equal to acc_in_smem; kept for the layout arithmetic)
@@ -102,7 +103,7 @@ __host__ __device__ inline long long rank_slice(long long longest) {
 }
 
 // Shared-memory layout shared by host (sizing) and device (carving): bucket starts and
-// reference counts (NB + 1 each), the slab's list of large buckets, accumulators, run
+// reference counts (NB + 1 each, padded to 16 bytes), the slab's list of large buckets, accumulators, run
 // counters, elements.
 struct RankSmem {
     size_t hist_bytes, acc_bytes, cnt_bytes, elem_bytes, total;
@@ -114,7 +115,7 @@ struct RankSmem {
     __host__ __device__ RankSmem(int nb_max_log2, int G, int tie_warps, int acc_in_smem,
                                  int cnt_in_smem, int elem_cap, int key_bytes) {
         const size_t NB = size_t(1) << nb_max_log2;
-        hist_bytes = align16((2 * (NB + 1) + big_list(elem_cap)) * 4);
+        hist_bytes = align16((2 * (NB + 4) + big_list(elem_cap)) * 4);
         acc_bytes = acc_in_smem ? align16(size_t(G) * 24) : 0;
         cnt_bytes = cnt_in_smem ? align16(size_t(tie_warps) * cnt_words(G) * 4) : 0;
         elem_bytes = align16(size_t(elem_cap) * (key_bytes + 4));
@@ -186,30 +187,67 @@ template <int NT>
 __device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint32_t* wsy,
                             uint32_t* xmax) {
     // exclusive prefix sums of x[0..L) and y[0..L) in place; x[L], y[L] = totals;
-    // *xmax = max x[i] (the caller zeroes it before)
+    // *xmax = max x[i] (the caller zeroes it before). x and y are 16-byte aligned; a thread
+    // owns `per` consecutive entries, moved with 128-bit accesses when per is 4 or 8.
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int per = (L + NT - 1) / NT;
-    const int beg = min(L, tid * per), end = min(L, beg + per);
+    const int beg = min(L, tid * per), cnt = min(L, beg + per) - beg;
+    uint32_t vx[8], vy[8];
+    if (cnt == 8 || cnt == 4) {
+        const uint4 a0 = *reinterpret_cast<const uint4*>(x + beg);
+        const uint4 b0 = *reinterpret_cast<const uint4*>(y + beg);
+        vx[0] = a0.x; vx[1] = a0.y; vx[2] = a0.z; vx[3] = a0.w;
+        vy[0] = b0.x; vy[1] = b0.y; vy[2] = b0.z; vy[3] = b0.w;
+        if (cnt == 8) {
+            const uint4 a1 = *reinterpret_cast<const uint4*>(x + beg + 4);
+            const uint4 b1 = *reinterpret_cast<const uint4*>(y + beg + 4);
+            vx[4] = a1.x; vx[5] = a1.y; vx[6] = a1.z; vx[7] = a1.w;
+            vy[4] = b1.x; vy[5] = b1.y; vy[6] = b1.z; vy[7] = b1.w;
+        } else {
+#pragma unroll
+            for (int i = 4; i < 8; ++i) { vx[i] = 0u; vy[i] = 0u; }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            vx[i] = i < cnt ? x[beg + i] : 0u;
+            vy[i] = i < cnt ? y[beg + i] : 0u;
+        }
+    }
     uint32_t sx = 0, sy = 0, mx = 0;
-    for (int i = beg; i < end; ++i) { sx += x[i]; sy += y[i]; mx = max(mx, x[i]); }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { sx += vx[i]; sy += vy[i]; mx = max(mx, vx[i]); }
     mx = __reduce_max_sync(0xffffffffu, mx);
     if (lane == 0 && mx) atomicMax(xmax, mx);
     const uint32_t ix = warp_incl_scan(sx), iy = warp_incl_scan(sy);
     if (lane == 31) { wsx[warp] = ix; wsy[warp] = iy; }
     __syncthreads();
     if (warp == 0) {
-        const uint32_t vx = lane < NT / 32 ? wsx[lane] : 0u;
-        const uint32_t vy = lane < NT / 32 ? wsy[lane] : 0u;
-        const uint32_t px = warp_incl_scan(vx), py = warp_incl_scan(vy);
-        if (lane < NT / 32) { wsx[lane] = px - vx; wsy[lane] = py - vy; }
+        const uint32_t ux = lane < NT / 32 ? wsx[lane] : 0u;
+        const uint32_t uy = lane < NT / 32 ? wsy[lane] : 0u;
+        const uint32_t px = warp_incl_scan(ux), py = warp_incl_scan(uy);
+        if (lane < NT / 32) { wsx[lane] = px - ux; wsy[lane] = py - uy; }
         if (lane == 31) { x[L] = px; y[L] = py; }
     }
     __syncthreads();
     uint32_t ox = wsx[warp] + ix - sx, oy = wsy[warp] + iy - sy;
-    for (int i = beg; i < end; ++i) {
-        const uint32_t tx = x[i], ty = y[i];
-        x[i] = ox; ox += tx;
-        y[i] = oy; oy += ty;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t tx = vx[i], ty = vy[i];
+        vx[i] = ox; ox += tx;
+        vy[i] = oy; oy += ty;
+    }
+    if (cnt == 8 || cnt == 4) {
+        *reinterpret_cast<uint4*>(x + beg) = make_uint4(vx[0], vx[1], vx[2], vx[3]);
+        *reinterpret_cast<uint4*>(y + beg) = make_uint4(vy[0], vy[1], vy[2], vy[3]);
+        if (cnt == 8) {
+            *reinterpret_cast<uint4*>(x + beg + 4) = make_uint4(vx[4], vx[5], vx[6], vx[7]);
+            *reinterpret_cast<uint4*>(y + beg + 4) = make_uint4(vy[4], vy[5], vy[6], vy[7]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (i < cnt) { x[beg + i] = vx[i]; y[beg + i] = vy[i]; }
     }
     __syncthreads();
 }
@@ -586,8 +624,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     const int cw = RankSmem::cnt_words(G);
 
     uint32_t* hall = reinterpret_cast<uint32_t*>(smem);  // bucket start (after the scan)
-    uint32_t* href = hall + NBMAX + 1;                   // reference elements below a bucket
-    uint32_t* biglist = href + NBMAX + 1;                // large buckets of the current slab
+    uint32_t* href = hall + NBMAX + 4;                   // reference elements below a bucket
+    uint32_t* biglist = href + NBMAX + 4;                // large buckets of the current slab
     const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(a.elem_smem_cap);
     unsigned char* accb;
     uint32_t* cnt_base;
