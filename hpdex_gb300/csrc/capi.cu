@@ -152,7 +152,8 @@ struct hpdex_plan {
     DevBuf<uint32_t> n1, n2;  // zero_handling = none
     // rank scratch: decoded column and bucket-ordered slab, one slice per CTA each
     DevBuf<unsigned char> dk, ek;
-    DevBuf<uint32_t> dg, eg;
+    DevBuf<unsigned char> dg, eg;
+    DevBuf<unsigned char> gidc;  // group of each row in the rank kernel's group type
     DevBuf<unsigned char> acc;
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
@@ -293,7 +294,8 @@ int configure_rank(hpdex_plan* p) {
     if (L.total + 16384 > budget) { acc_in = cnt_in = 0; L = RankSmem(nbl, G, tie_warps, 0, 0, 0, kb); }
     if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
     const size_t left = budget - L.total;
-    int cap = (int)std::min<size_t>(left / (kb + 5), (size_t)1 << 30);  // + big-list entry share
+    const int gb = group_bytes(acc_in);
+    int cap = (int)std::min<size_t>(left / (kb + gb + 1), (size_t)1 << 30);  // + big-list entry share
     cap = std::max(0, cap - 8) & ~7;
     L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
     p->rank_smem = L.total;
@@ -307,11 +309,12 @@ int configure_rank(hpdex_plan* p) {
     const long long slice = rank_slice(m->max_col_nnz);
     const size_t nctas = (size_t)p->rank_grid;
     TRY(p->dk.alloc(nctas * slice * kb));
-    TRY(p->dg.alloc(nctas * slice));
+    TRY(p->dg.alloc(nctas * slice * gb));
     if ((long long)cap < m->max_col_nnz) {
         TRY(p->ek.alloc(nctas * slice * kb));
-        TRY(p->eg.alloc(nctas * slice));
+        TRY(p->eg.alloc(nctas * slice * gb));
     }
+    TRY(p->gidc.alloc((size_t)std::max<long long>(m->n_rows, 1) * gb));
     if (!acc_in) TRY(p->acc.alloc(nctas * 24 * (size_t)G));
     TRY(p->cnt.alloc(nctas * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
 
@@ -325,7 +328,7 @@ int configure_rank(hpdex_plan* p) {
     a.n_rows = m->n_rows;
     a.n_cols = (int32_t)m->n_cols;
     a.G = G;
-    a.gid = p->gid.p;
+    a.group_of_row = p->gidc.p;
     a.order = p->order.p;
     a.queue = p->queue.p;
     a.single_gene = -1;
@@ -493,6 +496,17 @@ int check_device_errors(hpdex_plan* p) {
 // Rank kernel(s) for one run; batched = persistent + queue, plain = one launch per gene.
 int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
     if (p->m->n_cols == 0) return HPDEX_OK;
+    // group ids in the rank kernel's type (16-bit when its accumulators are in shared memory)
+    {
+        const long long R = p->m->n_rows;
+        const int grid = (int)std::max<long long>(1, std::min<long long>((R + 255) / 256, (long long)p->m->dev.sms * 8));
+        if (p->ra.acc_in_smem)
+            prepare_group_ids_kernel<uint16_t><<<grid, 256, 0, s>>>(p->gid.p, R, (int32_t)p->G, reinterpret_cast<uint16_t*>(p->gidc.p));
+        else
+            prepare_group_ids_kernel<uint32_t><<<grid, 256, 0, s>>>(p->gid.p, R, (int32_t)p->G, reinterpret_cast<uint32_t*>(p->gidc.p));
+        CUDA_TRY(cudaGetLastError());
+        *launches += 1;
+    }
     if (mode == HPDEX_MODE_BATCHED) {
         CUDA_TRY(cudaMemsetAsync(p->queue.p, 0, sizeof(int32_t), s));
         p->ra.single_gene = -1;
@@ -949,7 +963,8 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     const int tie_warps = kRankThreads / 32;
     RankSmem L(nbl, G, tie_warps, 1, 1, 0, kb);
     if (L.total + 16384 > budget) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: layout does not fit");
-    int cap = (int)std::min<size_t>((budget - L.total) / (kb + 5), (size_t)1 << 30);
+    const int gb = group_bytes(1);
+    int cap = (int)std::min<size_t>((budget - L.total) / (kb + gb + 1), (size_t)1 << 30);
     cap = std::max(0, cap - 8) & ~7;
     L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
     int blocks = 0;
@@ -959,21 +974,28 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     // per CTA and warp: run counters (packed, and 32-bit for very large buckets)
     uint32_t* cnt_glob = reinterpret_cast<uint32_t*>(
         take(sizeof(uint32_t) * (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
+    // group of each row, 16-bit
+    uint16_t* gidc = reinterpret_cast<uint16_t*>(take((size_t)std::max<long long>(n_rows, 1) * gb));
     if (off > kNoAllocScratchBytes) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: scratch exhausted");
     // per CTA: a decoded copy of the current column and, for columns larger than the
     // shared-memory capacity, a bucket-ordered slab slice
     const int nslices = (long long)longest > cap ? 2 : 1;
     off = (off + 127) & ~(size_t)127;  // slices in whole 128-byte lines
     const size_t left = off + 512 * (size_t)grid < kNoAllocScratchBytes ? kNoAllocScratchBytes - off - 512 * (size_t)grid : 0;
-    const long long slice = (long long)(left / ((size_t)grid * nslices * (kb + 4))) & ~31ll;
+    const long long slice = (long long)(left / ((size_t)grid * nslices * (kb + gb))) & ~63ll;
     if (rank_slice((long long)longest) > slice)
         return fail(HPDEX_ERR_UNSUPPORTED,
                     "hpdex_mannwhitneyu_noalloc: a column holds %llu entries, above the %lld the "
-                    "fixed scratch allows at this size", longest, slice - 71);
+                    "fixed scratch allows at this size", longest, slice);
     void* dk = take((size_t)grid * slice * kb);
-    uint32_t* dg = reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4));
+    void* dg = take((size_t)grid * slice * gb);
     void* ek = nslices == 2 ? take((size_t)grid * slice * kb) : nullptr;
-    uint32_t* eg = nslices == 2 ? reinterpret_cast<uint32_t*>(take((size_t)grid * slice * 4)) : nullptr;
+    void* eg = nslices == 2 ? take((size_t)grid * slice * gb) : nullptr;
+    {
+        const int pg = (int)std::max<long long>(1, std::min<long long>((n_rows + 255) / 256, (long long)nd->info.sms * 8));
+        prepare_group_ids_kernel<uint16_t><<<pg, 256, 0, s>>>(d_group_id, n_rows, G, gidc);
+        CUDA_TRY(cudaGetLastError());
+    }
 
     TRY(dispatch_dtype<NoAllocKeyRange>(dtype, d_data, d_indptr, (int32_t)C, kmin, kmax, has_zero, s));
     RankArgs a{};
@@ -986,7 +1008,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     a.n_rows = n_rows;
     a.n_cols = (int32_t)C;
     a.G = G;
-    a.gid = d_group_id;
+    a.group_of_row = gidc;
     a.order = order;
     a.queue = queue;
     a.single_gene = -1;

@@ -43,6 +43,7 @@
 #pragma once
 #include <climits>
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -60,7 +61,8 @@ struct RankArgs {
     int64_t n_rows;
     int32_t n_cols;
     int32_t G;                 // n_targets + 1
-    const int32_t* gid;        // [n_rows]
+    const void* group_of_row;  // [n_rows] group of each row in the kernel's group type
+                               // (GroupType below), all ones for rows in no group
     const int32_t* order;      // genes in processing order [n_cols]
     int32_t* queue;            // work counter (batched form)
     int32_t single_gene;       // >= 0: plain form, this gene only
@@ -76,10 +78,10 @@ struct RankArgs {
                                //      entries than rows (duplicate row ids)
     // global scratch, one slice of `slice` elements per CTA for each of:
     void* dk_global;           // decoded keys of the current gene, at the entries' positions
-    uint32_t* dg_global;       // decoded groups (kInvalid: not stored)
+    void* dg_global;           // decoded groups (group type; all ones: not stored)
     void* ek_global;           // bucket-ordered elements of a slab too big for shared memory
-    uint32_t* eg_global;
-    long long slice;           // rank_slice(longest column): multiple of 32 elements
+    void* eg_global;
+    long long slice;           // rank_slice(longest column): multiple of 64 elements
     unsigned char* acc_global; // per CTA 24*G bytes when the accumulators are not in SMEM
     uint32_t* cnt_global;      // per CTA and warp: packed counters (when not in SMEM), then
                                // G 32-bit counters (buckets of more than 65535 elements)
@@ -95,11 +97,16 @@ constexpr int kSmallBucket = 8;    // 2..8: four buckets per warp round
 constexpr int kMediumBucket = 32;  // 9..32: one warp round
 constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum per bucket
 constexpr uint32_t kInvalid = 0xffffffffu;
-// Scratch slice per CTA: the longest column plus the 4-entry alignment offset, in whole
-// 128-byte lines of 32-bit elements (discard.global.L2 works on lines, so no line of a
-// slice is shared with another CTA's slice).
+// Group ids inside the kernel: 16-bit when the accumulators are in shared memory (which
+// bounds G far below 65535), else 32-bit; all ones marks an entry outside every group.
+template <bool ACC_SMEM>
+using GroupType = std::conditional_t<ACC_SMEM, uint16_t, uint32_t>;
+__host__ __device__ inline int group_bytes(int acc_in_smem) { return acc_in_smem ? 2 : 4; }
+
+// Scratch slice per CTA: the longest column in whole 128-byte lines of 16-bit elements
+// (discard.global.L2 works on lines, so no line of a slice is shared with another CTA's).
 __host__ __device__ inline long long rank_slice(long long longest) {
-    return (longest + 40 + 31) & ~31ll;
+    return ((longest > 0 ? longest : 1) + 63) & ~63ll;
 }
 
 // Shared-memory layout shared by host (sizing) and device (carving): bucket starts and
@@ -118,7 +125,7 @@ struct RankSmem {
         hist_bytes = align16((2 * (NB + 4) + big_list(elem_cap)) * 4);
         acc_bytes = acc_in_smem ? align16(size_t(G) * 24) : 0;
         cnt_bytes = cnt_in_smem ? align16(size_t(tie_warps) * cnt_words(G) * 4) : 0;
-        elem_bytes = align16(size_t(elem_cap) * (key_bytes + 4));
+        elem_bytes = align16(size_t(elem_cap) * (key_bytes + group_bytes(acc_in_smem)));
         total = hist_bytes + acc_bytes + cnt_bytes + elem_bytes;
     }
 };
@@ -253,46 +260,13 @@ __device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint
 }
 
 // Streaming (evict-first) loads of the matrix: each entry is read once per run.
-__device__ __forceinline__ int4 ld_stream(const int4* p) { return __ldcs(p); }
-// 4 consecutive values starting at a 4-element-aligned position, one or two vector loads
-template <class V, bool STREAM>
-__device__ __forceinline__ void load4(const V* p, V (&v)[4]) {
-    if constexpr (sizeof(V) == 4) {
-        const uint4 u = STREAM ? __ldcs(reinterpret_cast<const uint4*>(p)) : *reinterpret_cast<const uint4*>(p);
-        v[0] = __builtin_bit_cast(V, u.x); v[1] = __builtin_bit_cast(V, u.y);
-        v[2] = __builtin_bit_cast(V, u.z); v[3] = __builtin_bit_cast(V, u.w);
-    } else if constexpr (sizeof(V) == 8) {
-        const ulonglong2* q = reinterpret_cast<const ulonglong2*>(p);
-        const ulonglong2 a = STREAM ? __ldcs(q) : q[0];
-        const ulonglong2 b = STREAM ? __ldcs(q + 1) : q[1];
-        v[0] = __builtin_bit_cast(V, a.x); v[1] = __builtin_bit_cast(V, a.y);
-        v[2] = __builtin_bit_cast(V, b.x); v[3] = __builtin_bit_cast(V, b.y);
-    } else if constexpr (sizeof(V) == 2) {
-        const uint2 u = STREAM ? __ldcs(reinterpret_cast<const uint2*>(p)) : *reinterpret_cast<const uint2*>(p);
-        v[0] = __builtin_bit_cast(V, (uint16_t)(u.x & 0xffffu));
-        v[1] = __builtin_bit_cast(V, (uint16_t)(u.x >> 16));
-        v[2] = __builtin_bit_cast(V, (uint16_t)(u.y & 0xffffu));
-        v[3] = __builtin_bit_cast(V, (uint16_t)(u.y >> 16));
-    } else {
-        const uint32_t u = STREAM ? __ldcs(reinterpret_cast<const unsigned int*>(p)) : *reinterpret_cast<const uint32_t*>(p);
-        v[0] = __builtin_bit_cast(V, (uint8_t)(u & 0xffu));
-        v[1] = __builtin_bit_cast(V, (uint8_t)((u >> 8) & 0xffu));
-        v[2] = __builtin_bit_cast(V, (uint8_t)((u >> 16) & 0xffu));
-        v[3] = __builtin_bit_cast(V, (uint8_t)(u >> 24));
-    }
+template <class V>
+__device__ __forceinline__ V ld_stream(const V* p) {
+    if constexpr (sizeof(V) == 8) return __builtin_bit_cast(V, __ldcs(reinterpret_cast<const unsigned long long*>(p)));
+    else if constexpr (sizeof(V) == 4) return __builtin_bit_cast(V, __ldcs(reinterpret_cast<const unsigned int*>(p)));
+    else if constexpr (sizeof(V) == 2) return __builtin_bit_cast(V, __ldcs(reinterpret_cast<const unsigned short*>(p)));
+    else return __builtin_bit_cast(V, __ldcs(reinterpret_cast<const unsigned char*>(p)));
 }
-
-// 4 keys at a 4-aligned position (vector stores)
-template <class K>
-__device__ __forceinline__ void store4(K* p, const K (&k)[4]) {
-    if constexpr (sizeof(K) == 4) {
-        *reinterpret_cast<uint4*>(p) = make_uint4(k[0], k[1], k[2], k[3]);
-    } else {
-        reinterpret_cast<ulonglong2*>(p)[0] = make_ulonglong2(k[0], k[1]);
-        reinterpret_cast<ulonglong2*>(p)[1] = make_ulonglong2(k[2], k[3]);
-    }
-}
-
 // Per-warp, per-group counters of a run, 16 bits each (two groups per 32-bit word). A run
 // never counts more than 65535 elements of one group here: buckets with more than 65535
 // elements are resolved with 32-bit counters instead.
@@ -645,14 +619,16 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     uint32_t* wide_base = cnt_glob + (size_t)a.tie_warps * cw;
     uint32_t* cnt = cnt_base + (size_t)warp * cw;
     uint32_t* wide_cnt = wide_base + (size_t)warp * G;
+    using GT = GroupType<ACC_SMEM>;
+    constexpr uint32_t kNoGroup = ACC_SMEM ? 0xffffu : 0xffffffffu;
     K* ek_s = reinterpret_cast<K*>(smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes);
-    uint32_t* eg_s = reinterpret_cast<uint32_t*>(ek_s + a.elem_smem_cap);
+    GT* eg_s = reinterpret_cast<GT*>(ek_s + a.elem_smem_cap);
     K* dk = reinterpret_cast<K*>(a.dk_global) + (size_t)blockIdx.x * a.slice;
-    uint32_t* dg = a.dg_global + (size_t)blockIdx.x * a.slice;
+    GT* dg = reinterpret_cast<GT*>(a.dg_global) + (size_t)blockIdx.x * a.slice;
     K* ek_g = reinterpret_cast<K*>(a.ek_global) + (size_t)blockIdx.x * a.slice;
-    uint32_t* eg_g = a.eg_global + (size_t)blockIdx.x * a.slice;
+    GT* eg_g = reinterpret_cast<GT*>(a.eg_global) + (size_t)blockIdx.x * a.slice;
 
-    const int32_t* gidp = a.gid;
+    const GT* gidp = reinterpret_cast<const GT*>(a.group_of_row);
     const uint32_t nrows = (uint32_t)a.n_rows;
 
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
@@ -682,13 +658,12 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         if (c < 0) break;
         const long long p0 = a.indptr[c];
         const uint32_t nraw = (uint32_t)(a.indptr[c + 1] - p0);
-        // entries of this gene, re-based: entry i is rows[i], data[i]; the decoded copy of
-        // entry i sits at dk/dg[i + off] where off = p0 % 4 keeps vector accesses aligned
+        // entries of this gene, re-based: entry i is rows[i], data[i]; its decoded copy is
+        // dk/dg[i]. Passes over the entries go by warp tiles of 128: lane l of a warp takes
+        // entries t + l + 32k (k < 4), so that neighbouring lanes read neighbouring entries
+        // and their group-id gathers (rows of one column ascend) share L2 sectors.
         const int32_t* rows = a.rows + p0;
         const V* data = reinterpret_cast<const V*>(a.data) + p0;
-        const uint32_t off = (uint32_t)(p0 & 3);
-        const uint32_t ia = min(nraw, (4u - off) & 3u);           // aligned body [ia, ib)
-        const uint32_t ib = ia + ((nraw - ia) & ~3u);
 
         // ---- bucket function from the column's key range ----
         K kmin = (K)a.col_kmin[c], kmax = (K)a.col_kmax[c];
@@ -710,77 +685,57 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
-        auto count = [&](uint32_t g, K key, V v) {
-            if (g) red_add<ACC_SMEM>(&nz[g], 1u);
-            else ++nref_local;
-            if (zh == ZH_MIX && Val<V>::neg(v)) red_add<ACC_SMEM>(&ng[g], 1u);
-            const uint32_t b = (uint32_t)((key - kmin) >> shift);
-            red_add<true>(&hall[b], 1u);
-            if (g == 0) red_add<true>(&href[b], 1u);
-        };
-        auto scalar1 = [&](uint32_t i) {
-            const int32_t r = rows[i];
-            const V v = data[i];
-            uint32_t g = kInvalid;
-            K key = K(0);
-            if ((uint32_t)r < nrows) {  // negative ids wrap above n_rows
-                const int gr = __ldg(gidp + r);
-                if ((unsigned)gr < (unsigned)G && Val<V>::finite(v) &&
-                    (zh == ZH_NONE || !Val<V>::zero(v))) {
-                    g = (uint32_t)gr;
-                    key = Val<V>::key(v);
-                }
-            }
-            dk[i + off] = key;
-            dg[i + off] = g;
-            if (g != kInvalid) count(g, key, v);
-        };
-        for (uint32_t i = tid; i < ia; i += NT) scalar1(i);
         {
-            uint32_t q = ia + 4u * tid;
-            if (q < ib) {
-                int4 r = ld_stream(reinterpret_cast<const int4*>(rows + q));
+            uint32_t t = 128u * (uint32_t)warp;
+            if (t < nraw) {
+                int32_t r[4];
                 V v[4];
-                load4<V, true>(data + q, v);
-                for (;;) {
-                    const uint32_t qn = q + 4u * NT;
-                    const bool more = qn < ib;
-                    int4 rn = make_int4(-1, -1, -1, -1);
-                    V vn[4] = {V(0), V(0), V(0), V(0)};
-                    if (more) {
-                        rn = ld_stream(reinterpret_cast<const int4*>(rows + qn));
-                        load4<V, true>(data + qn, vn);
-                    }
-                    const int32_t rr[4] = {r.x, r.y, r.z, r.w};
-                    // all four group-id gathers in flight before any of them is tested
-                    int gl[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        gl[k] = __ldg(gidp + ((uint32_t)rr[k] < nrows ? rr[k] : 0));
-                    K key[4];
-                    uint32_t g[4];
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t i = t + 32u * k + lane;
+                    r[k] = i < nraw ? __ldcs(rows + i) : -1;
+                    v[k] = i < nraw ? ld_stream(data + i) : V(0);
+                }
+                for (;;) {
+                    const uint32_t tn = t + 4u * NT;
+                    const bool more = tn < nraw;
+                    int32_t rn[4];
+                    V vn[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        const bool ok = (uint32_t)rr[k] < nrows && (unsigned)gl[k] < (unsigned)G &&
-                                        Val<V>::finite(v[k]) &&
-                                        (zh == ZH_NONE || !Val<V>::zero(v[k]));
-                        key[k] = ok ? Val<V>::key(v[k]) : K(0);
-                        g[k] = ok ? (uint32_t)gl[k] : kInvalid;
+                        const uint32_t i = tn + 32u * k + lane;
+                        rn[k] = (more && i < nraw) ? __ldcs(rows + i) : -1;
+                        vn[k] = (more && i < nraw) ? ld_stream(data + i) : V(0);
                     }
-                    store4<K>(dk + q + off, key);
-                    *reinterpret_cast<uint4*>(dg + q + off) = make_uint4(g[0], g[1], g[2], g[3]);
+                    // all four group-id gathers in flight before any of them is tested
+                    uint32_t gl[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (g[k] != kInvalid) count(g[k], key[k], v[k]);
-                    if (!more) break;
-                    q = qn;
-                    r = rn;
+                        gl[k] = (uint32_t)r[k] < nrows ? (uint32_t)__ldg(gidp + r[k]) : kNoGroup;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) v[k] = vn[k];
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t i = t + 32u * k + lane;
+                        const bool ok = gl[k] != kNoGroup && Val<V>::finite(v[k]) &&
+                                        (zh == ZH_NONE || !Val<V>::zero(v[k]));
+                        const K key = ok ? Val<V>::key(v[k]) : K(0);
+                        const uint32_t g = ok ? gl[k] : kNoGroup;
+                        if (i < nraw) { dk[i] = key; dg[i] = (GT)g; }
+                        if (ok) {
+                            if (g) red_add<ACC_SMEM>(&nz[g], 1u);
+                            else ++nref_local;
+                            if (zh == ZH_MIX && Val<V>::neg(v[k])) red_add<ACC_SMEM>(&ng[g], 1u);
+                            const uint32_t b = (uint32_t)((key - kmin) >> shift);
+                            red_add<true>(&hall[b], 1u);
+                            if (g == 0) red_add<true>(&href[b], 1u);
+                        }
+                    }
+                    if (!more) break;
+                    t = tn;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) { r[k] = rn[k]; v[k] = vn[k]; }
                 }
             }
         }
-        for (uint32_t i = ib + tid; i < nraw; i += NT) scalar1(i);
         nref_local = __reduce_add_sync(0xffffffffu, nref_local);
         if (lane == 0 && nref_local) red_add<ACC_SMEM>(&nz[0], nref_local);
         __syncthreads();
@@ -825,36 +780,33 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             // ---- pass 2 (L2): scatter this slab's decoded elements into bucket order ----
             if (cnt_slab) {
                 const bool all = nslabs == 1u;
-                auto place = [&](K key, uint32_t g) {
-                    if (g == kInvalid) return;
-                    const uint32_t b = (uint32_t)((key - kmin) >> shift);
-                    if (!all && (b < blo || b >= bhi)) return;
-                    const uint32_t pos = atom_add<true>(&hall[b], 1u) - base;
-                    if (in_smem) { ek_s[pos] = key; eg_s[pos] = g; }
-                    else { ek_g[pos] = key; eg_g[pos] = g; }
-                };
-                for (uint32_t i = tid; i < ia; i += NT) place(dk[i + off], dg[i + off]);
-                uint32_t q = ia + 4u * tid;
-                if (q < ib) {
+                uint32_t t = 128u * (uint32_t)warp;
+                if (t < nraw) {
                     K k4[4];
-                    load4<K, false>(dk + q + off, k4);
-                    uint4 g4 = *reinterpret_cast<const uint4*>(dg + q + off);
+                    uint32_t g4[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t i = t + 32u * k + lane;
+                        k4[k] = i < nraw ? dk[i] : K(0);
+                        g4[k] = i < nraw ? (uint32_t)dg[i] : kNoGroup;
+                    }
                     for (;;) {
-                        const uint32_t qn = q + 4u * NT;
-                        const bool more = qn < ib;
-                        K kn[4] = {K(0), K(0), K(0), K(0)};
-                        uint4 gn = make_uint4(kInvalid, kInvalid, kInvalid, kInvalid);
-                        if (more) {
-                            load4<K, false>(dk + qn + off, kn);
-                            gn = *reinterpret_cast<const uint4*>(dg + qn + off);
+                        const uint32_t tn = t + 4u * NT;
+                        const bool more = tn < nraw;
+                        K kn[4];
+                        uint32_t gn[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            const uint32_t i = tn + 32u * k + lane;
+                            kn[k] = (more && i < nraw) ? dk[i] : K(0);
+                            gn[k] = (more && i < nraw) ? (uint32_t)dg[i] : kNoGroup;
                         }
-                        const uint32_t gg[4] = {g4.x, g4.y, g4.z, g4.w};
                         uint32_t bb[4];
                         bool in[4];
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
                             bb[k] = (uint32_t)((k4[k] - kmin) >> shift);
-                            in[k] = gg[k] != kInvalid && (all || (bb[k] >= blo && bb[k] < bhi));
+                            in[k] = g4[k] != kNoGroup && (all || (bb[k] >= blo && bb[k] < bhi));
                         }
                         uint32_t pos[4];
 #pragma unroll
@@ -863,23 +815,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
                             if (!in[k]) continue;
-                            if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = gg[k]; }
-                            else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = gg[k]; }
+                            if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = (GT)g4[k]; }
+                            else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = (GT)g4[k]; }
                         }
                         if (!more) break;
-                        q = qn;
-                        g4 = gn;
+                        t = tn;
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) k4[k] = kn[k];
+                        for (int k = 0; k < 4; ++k) { k4[k] = kn[k]; g4[k] = gn[k]; }
                     }
                 }
-                for (uint32_t i = ib + tid; i < nraw; i += NT) place(dk[i + off], dg[i + off]);
             }
             __syncthreads();
             if (slab + 1u == nslabs) {
                 // the decoded copy is dead: drop its lines from L2 instead of writing them back
-                l2_discard<NT>(dk, (size_t)(nraw + off) * sizeof(K));
-                l2_discard<NT>(dg, (size_t)(nraw + off) * 4u);
+                l2_discard<NT>(dk, (size_t)nraw * sizeof(K));
+                l2_discard<NT>(dg, (size_t)nraw * sizeof(GT));
             }
 
             // ---- rank ----
@@ -932,6 +882,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             a.tie[idx] = a.tie_correction ? (double)ties : 0.0;
         }
         __syncthreads();
+    }
+}
+
+// Group of every row in the rank kernel's group type: the caller's id when it names a group
+// in [0, G), else all ones (the reference skips such rows, mannwhitneyu.cpp:914-926).
+template <class GT>
+__global__ void prepare_group_ids_kernel(const int32_t* gid, long long n_rows, int32_t G, GT* out) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += stride) {
+        const int32_t g = gid[r];
+        out[r] = (g >= 0 && g < G) ? (GT)g : (GT)~GT(0);
     }
 }
 
