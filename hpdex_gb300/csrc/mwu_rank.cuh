@@ -23,8 +23,8 @@
 //           slab made of one bucket larger than half the capacity uses a global slice);
 //           after the last slab the decoded copy is dropped from L2 without write-back
 //           (discard.global.L2)
-//   rank    32-bucket chunks to all warps: singleton buckets add one term; buckets of 2..8
-//           elements are resolved four at a time per warp, 9..32 one per warp: reference
+//   rank    32-bucket chunks to all warps: singleton buckets add one term; buckets of 2..32
+//           elements are packed whole into 32-lane warp rounds: reference
 //           lanes are broadcast to count smaller / equal reference keys, per-warp group
 //           counters find repeated (key, group) pairs; larger buckets go to a list that
 //           warps drain one bucket at a time with per-warp group counters: one
@@ -93,8 +93,7 @@ struct RankArgs {
     int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
 };
 
-constexpr int kSmallBucket = 8;    // 2..8: four buckets per warp round
-constexpr int kMediumBucket = 32;  // 9..32: one warp round
+constexpr int kMediumBucket = 32;  // 2..32: packed whole into warp rounds
 constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum per bucket
 constexpr uint32_t kInvalid = 0xffffffffu;
 // Group ids inside the kernel: 16-bit when the accumulators are in shared memory (which
@@ -490,12 +489,14 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
 
 // Rank phase of one slab: elements [0, cnt) in bucket order in ek/eg, buckets [blo, bhi)
 // starting at `base` in the gene's bucket order (hall[b - 1] = start of bucket b).
+// Buckets of 2..32 elements are packed whole, in bucket order, into rounds of up to 32
+// lanes; `tbl` (32 bytes per warp) maps the k-th such bucket of a chunk to its lane.
 template <class K, bool SH, class EK, class EG>
 __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi, uint32_t base,
                           const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
                           uint32_t* s_bigi, const Acc& acc, uint32_t* cnt, uint32_t* wide_cnt,
-                          unsigned long long& tref) {
+                          uint8_t* tbl, unsigned long long& tref) {
     const int lane = threadIdx.x & 31;
     const uint32_t nchunks = (bhi - blo + 31u) / 32u;
     for (;;) {
@@ -521,39 +522,46 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             if (slot < biglist_cap) biglist[slot] = b;
             else spill = true;  // list full (the sizing rules this out): resolve below
         }
-        // buckets of 2..8 elements: four per round, 8 lanes each
-        unsigned smask = __ballot_sync(0xffffffffu, m >= 2u && m <= (uint32_t)kSmallBucket);
-        while (smask) {
-            int src[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                src[q] = smask ? __ffs((int)smask) - 1 : -1;
-                if (smask) smask &= smask - 1u;
+        // buckets of 2..32 elements, packed whole into rounds: a round takes the next
+        // buckets (in order) whose sizes sum to at most 32; lane j holds the round's j-th
+        // element, and the round's bucket boundaries come from the buckets' exclusive
+        // prefix P over the packable sizes
+        const bool pk = m >= 2u && m <= (uint32_t)kMediumBucket;
+        unsigned rem = __ballot_sync(0xffffffffu, pk);
+        if (rem) {
+            const uint32_t mp = pk ? m : 0u;
+            const uint32_t P = warp_incl_scan(mp) - mp;
+            __syncwarp();  // the previous chunk's rounds have read the table
+            if (pk) tbl[__popc(rem & ((1u << lane) - 1u))] = (uint8_t)lane;
+            __syncwarp();
+            uint32_t ord0 = 0;  // packable buckets of this chunk resolved in earlier rounds
+            while (rem) {
+                const int f = __ffs((int)rem) - 1;
+                const uint32_t B0 = __shfl_sync(0xffffffffu, P, f);
+                const bool inr = ((rem >> lane) & 1u) && P + m - B0 <= 32u;
+                const unsigned I = __ballot_sync(0xffffffffu, inr);
+                const unsigned starts = __reduce_or_sync(0xffffffffu, inr ? (1u << (P - B0)) : 0u);
+                const int last = 31 - __clz((int)I);
+                const uint32_t total = __shfl_sync(0xffffffffu, P + m, last) - B0;
+                const bool active = (uint32_t)lane < total;
+                int src = lane;
+                if (active) src = tbl[ord0 + __popc(starts & ((2u << lane) - 1u)) - 1u];
+                const uint32_t sq = __shfl_sync(0xffffffffu, s0, src);
+                const uint32_t rq = __shfl_sync(0xffffffffu, rb, src);
+                const uint32_t pq = __shfl_sync(0xffffffffu, P, src) - B0;
+                const uint32_t mq = __shfl_sync(0xffffffffu, m, src);
+                K key = K(0);
+                uint32_t g = 0;
+                if (active) {
+                    const uint32_t e = (uint32_t)lane - pq;
+                    key = ek[sq + e];
+                    g = eg[sq + e];
+                }
+                const unsigned sub = (mq >= 32u ? 0xffffffffu : ((1u << mq) - 1u)) << pq;
+                resolve_round<K, SH>(active, key, g, sub, rq, acc, cnt, tref);
+                ord0 += __popc(I);
+                rem &= ~I;
             }
-            const int q = lane >> 3, e = lane & 7;
-            const int sl = src[q];
-            const uint32_t mq = __shfl_sync(0xffffffffu, m, sl < 0 ? 0 : sl);
-            const uint32_t sq = __shfl_sync(0xffffffffu, s0, sl < 0 ? 0 : sl);
-            const uint32_t rq = __shfl_sync(0xffffffffu, rb, sl < 0 ? 0 : sl);
-            const bool active = sl >= 0 && (uint32_t)e < mq;
-            K key = K(0);
-            uint32_t g = 0;
-            if (active) { key = ek[sq + e]; g = eg[sq + e]; }
-            resolve_round<K, SH>(active, key, g, 0xffu << (8 * q), rq, acc, cnt, tref);
-        }
-        // buckets of 9..32 elements: one round each
-        unsigned mmask = __ballot_sync(0xffffffffu, m > (uint32_t)kSmallBucket && m <= (uint32_t)kMediumBucket);
-        while (mmask) {
-            const int j = __ffs((int)mmask) - 1;
-            mmask &= mmask - 1u;
-            const uint32_t mj = __shfl_sync(0xffffffffu, m, j);
-            const uint32_t sj = __shfl_sync(0xffffffffu, s0, j);
-            const uint32_t rj = __shfl_sync(0xffffffffu, rb, j);
-            const bool active = (uint32_t)lane < mj;
-            K key = K(0);
-            uint32_t g = 0;
-            if (active) { key = ek[sj + lane]; g = eg[sj + lane]; }
-            resolve_round<K, SH>(active, key, g, 0xffffffffu, rj, acc, cnt, tref);
         }
         unsigned over = __ballot_sync(0xffffffffu, spill);
         while (over) {
@@ -589,6 +597,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     __shared__ unsigned long long s_tref;
     __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi;
     __shared__ uint32_t s_wsx[32], s_wsy[32];
+    __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = a.G, zh = a.zero_handling;
@@ -836,11 +845,11 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             if (in_smem)
                 rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
-                                       wide_cnt, tref);
+                                       wide_cnt, s_tbl[warp], tref);
             else
                 rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
-                                       wide_cnt, tref);
+                                       wide_cnt, s_tbl[warp], tref);
             __syncthreads();
             if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
             blo = bhi;
