@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -14,6 +15,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -62,21 +64,30 @@ struct DeviceInfo {
     int device = -1;
     int sms = 0;
     size_t smem_per_sm = 0, smem_optin = 0, smem_reserved = 0;
+    bool pageable_access = false;
 };
 
+// Properties of the current device, queried once per device and process.
 int device_info(DeviceInfo& d) {
+    static std::mutex mu;
+    static std::map<int, DeviceInfo> cache;
     int dev = 0;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
         return fail(HPDEX_ERR_CUDA, "no CUDA device is available (hpdex_gb300 has no CPU path)");
     CUDA_TRY(cudaGetDevice(&dev));
-    cudaDeviceProp p;
-    CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) { d = it->second; return HPDEX_OK; }
+    int v = 0;
     d.device = dev;
-    d.sms = p.multiProcessorCount;
-    d.smem_per_sm = p.sharedMemPerMultiprocessor;
-    d.smem_optin = p.sharedMemPerBlockOptin;
-    d.smem_reserved = p.reservedSharedMemPerBlock;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev)); d.sms = v;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)); d.smem_per_sm = (size_t)v;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)); d.smem_optin = (size_t)v;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev)); d.smem_reserved = (size_t)v;
+    // kernels may read and write pageable host memory directly (coherent host memory)
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev)); d.pageable_access = v != 0;
+    cache[dev] = d;
     return HPDEX_OK;
 }
 
@@ -132,7 +143,7 @@ struct hpdex_matrix {
     DevBuf<int32_t> rows;
     DevBuf<int64_t> indptr;
     DevBuf<unsigned long long> col_kmin, col_kmax;  // per-column key range (resident layout)
-    DevBuf<unsigned char> col_has_zero;
+    DevBuf<uint32_t> col_has_zero;
     std::vector<long long> col_nnz;  // host copy for scheduling
     long long max_col_nnz = 0;
     DeviceInfo dev;
@@ -206,12 +217,17 @@ int rank_status(cudaError_t e, const char* what) {
 
 template <class V>
 struct KeyRangeLaunch {
-    static int run(hpdex_matrix* m) {
-        const int threads = 256, wpb = threads / 32;
-        const int grid = (int)std::max<long long>(1, std::min<long long>((m->n_cols + wpb - 1) / wpb, 65535));
-        column_key_range_kernel<V><<<grid, threads>>>(reinterpret_cast<const V*>(m->data.p), m->indptr.p,
-                                                     (int32_t)m->n_cols, m->col_kmin.p, m->col_kmax.p,
-                                                     m->col_has_zero.p);
+    // key ranges of columns [0, w) of indptr (entries ~ a hint for the grid); resets them first
+    static int run(const void* data, const int64_t* indptr, long long w, unsigned long long* kmin,
+                   unsigned long long* kmax, uint32_t* hz, long long entries, int sms, cudaStream_t s) {
+        if (w <= 0) return HPDEX_OK;
+        CUDA_TRY(cudaMemsetAsync(kmin, 0xff, sizeof(unsigned long long) * w, s));
+        CUDA_TRY(cudaMemsetAsync(kmax, 0, sizeof(unsigned long long) * w, s));
+        CUDA_TRY(cudaMemsetAsync(hz, 0, sizeof(uint32_t) * w, s));
+        const long long per_block = 8ll * 32 * kRangePer;  // 256 threads
+        const int grid = (int)std::max<long long>(1, std::min<long long>((entries + per_block - 1) / per_block, (long long)sms * 16));
+        column_key_range_kernel<V><<<grid, 256, 0, s>>>(reinterpret_cast<const V*>(data), indptr, (int32_t)w,
+                                                       kmin, kmax, hz);
         CUDA_TRY(cudaGetLastError());
         return HPDEX_OK;
     }
@@ -266,7 +282,9 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
     TRY(m->col_kmax.alloc(std::max<long long>(m->n_cols, 1)));
     TRY(m->col_has_zero.alloc(std::max<long long>(m->n_cols, 1)));
     if (m->n_cols) {
-        TRY(dispatch_dtype<KeyRangeLaunch>(m->dtype, m));
+        TRY(dispatch_dtype<KeyRangeLaunch>(m->dtype, (const void*)m->data.p, (const int64_t*)m->indptr.p, m->n_cols,
+                                           m->col_kmin.p, m->col_kmax.p, m->col_has_zero.p, m->nnz, m->dev.sms,
+                                           (cudaStream_t)0));
         CUDA_TRY(cudaDeviceSynchronize());
     }
     m->col_nnz.resize((size_t)m->n_cols);
@@ -327,6 +345,7 @@ int configure_rank(hpdex_plan* p) {
     a.col_has_zero = m->col_has_zero.p;
     a.n_rows = m->n_rows;
     a.n_cols = (int32_t)m->n_cols;
+    a.n_order = (int32_t)m->n_cols;
     a.G = G;
     a.group_of_row = p->gidc.p;
     a.order = p->order.p;
@@ -361,6 +380,8 @@ int launch_pvalues_asymptotic(hpdex_plan* p, cudaStream_t s) {
     a.P = p->P.p;
     a.n = p->T * p->m->n_cols;
     a.n_cols = (int32_t)p->m->n_cols;
+    a.col_lo = 0;
+    a.col_w = (int32_t)p->m->n_cols;
     a.group_rows = p->d_group_rows.p;
     a.n1g = p->n1.p;
     a.n2t = p->n2.p;
@@ -522,6 +543,10 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
     }
     return HPDEX_OK;
 }
+
+int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
+                      int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
+                      int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out);
 
 }  // namespace
 
@@ -727,6 +752,9 @@ int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
     (void)threads;
     if (!opt) return fail(HPDEX_ERR_ARGUMENT, "options are NULL");
     if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    if (opt->method != HPDEX_EXACT)
+        return oneshot_pipelined(dtype, data, indices, indptr, n_rows, n_cols, nnz, group_id, n_targets, opt,
+                                 U1_out, P_out);
     hpdex_matrix* m = nullptr;
     TRY(hpdex_matrix_create(dtype, data, indices, indptr, n_rows, n_cols, nnz, &m));
     hpdex_plan* p = nullptr;
@@ -793,6 +821,187 @@ int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
 }
 
 }  // extern "C"
+
+// =======================================================================================
+// Pipelined one-shot call (asymptotic method).
+//
+// hpdex_mannwhitneyu receives the matrix in host memory. The columns are cut into chunks of
+// about equal nnz; a copy stream moves chunk k+1 (values, and int64 row ids into one of two
+// staging buffers) while the compute stream narrows the row ids of chunk k, computes its
+// column key ranges, ranks its genes (the persistent rank kernel over the chunk's genes,
+// longest first) and finishes its p-values. When the device can access pageable host
+// memory the p-value kernel writes U1 and P straight into the caller's arrays; otherwise
+// they are copied back at the end. Host<->device traffic is the bound of this call, so the
+// kernels run in the shadow of the copies except for the last chunk.
+// =======================================================================================
+namespace {
+
+constexpr int kPipelineChunks = 8;
+
+int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
+                      int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
+                      int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out) {
+    const size_t vs = dtype_size(dtype);
+    if (vs == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
+    if (!indptr || (nnz > 0 && (!data || !indices))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    TRY(validate_csc(indptr, n_cols, nnz, n_rows));
+    const long long C = n_cols;
+
+    // matrix shell: device buffers and host metadata; the entries arrive chunk by chunk
+    std::unique_ptr<hpdex_matrix> m(new hpdex_matrix());
+    m->dtype = dtype;
+    m->n_rows = n_rows;
+    m->n_cols = n_cols;
+    m->nnz = nnz;
+    TRY(device_info(m->dev));
+    TRY(m->data.alloc(std::max<size_t>(1, (size_t)nnz * vs)));
+    TRY(m->rows.alloc(std::max<long long>(1, nnz)));
+    TRY(m->indptr.alloc((size_t)C + 1));
+    TRY(m->col_kmin.alloc(std::max<long long>(C, 1)));
+    TRY(m->col_kmax.alloc(std::max<long long>(C, 1)));
+    TRY(m->col_has_zero.alloc(std::max<long long>(C, 1)));
+    CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t) * ((size_t)C + 1), cudaMemcpyHostToDevice));
+    m->col_nnz.resize((size_t)C);
+    for (long long c = 0; c < C; ++c) {
+        m->col_nnz[(size_t)c] = indptr[c + 1] - indptr[c];
+        m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
+    }
+    hpdex_plan* praw = nullptr;
+    TRY(hpdex_plan_create(m.get(), group_id, n_targets, opt, &praw));
+    std::unique_ptr<hpdex_plan> p(praw);
+    const long long T = p->T;
+    if (C == 0) return HPDEX_OK;
+
+    // chunks of about nnz / kPipelineChunks entries (whole columns)
+    std::vector<long long> cb{0};
+    for (int k = 1; k < kPipelineChunks; ++k) {
+        const long long target = nnz / kPipelineChunks * k;
+        const long long c = std::lower_bound(indptr, indptr + C + 1, target) - indptr;
+        if (c > cb.back() && c < C) cb.push_back(c);
+    }
+    cb.push_back(C);
+    const int K = (int)cb.size() - 1;
+    long long max_chunk = 0;
+    std::vector<int32_t> order((size_t)C);
+    for (int k = 0; k < K; ++k) {
+        max_chunk = std::max<long long>(max_chunk, (long long)(indptr[cb[k + 1]] - indptr[cb[k]]));
+        auto b = order.begin() + cb[k], e = order.begin() + cb[k + 1];
+        std::iota(b, e, (int32_t)cb[k]);
+        std::stable_sort(b, e, [&](int32_t x, int32_t y) { return m->col_nnz[(size_t)x] > m->col_nnz[(size_t)y]; });
+    }
+    CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
+    DevBuf<int32_t> queues;
+    DevBuf<long long> stage[2];
+    TRY(queues.alloc((size_t)K));
+    for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
+
+    // Output pages never written before (fresh numpy arrays) would fault one by one when the
+    // device writes them; a host thread touches them while the first chunk is in flight, and
+    // the compute stream waits for it before the first p-value kernel.
+    const bool direct = m->dev.pageable_access && U1_out && P_out;
+    std::atomic<int> touched{0};
+    struct Toucher {
+        std::thread t;
+        ~Toucher() { if (t.joinable()) t.join(); }
+    } toucher;
+    if (direct) {
+        const size_t bytes = sizeof(double) * (size_t)(T * C);
+        toucher.t = std::thread([U1_out, P_out, bytes, &touched] {
+            for (size_t o = 0; o < bytes; o += 4096) {
+                reinterpret_cast<volatile unsigned char*>(U1_out)[o] = 0;
+                reinterpret_cast<volatile unsigned char*>(P_out)[o] = 0;
+            }
+            touched.store(1, std::memory_order_release);
+        });
+    }
+    struct Res {  // streams and events of this call, released after both streams drained
+        cudaStream_t copy = nullptr;
+        std::vector<cudaEvent_t> ev;
+        cudaStream_t comp = nullptr;
+        ~Res() {
+            if (copy) cudaStreamSynchronize(copy);
+            if (comp) cudaStreamSynchronize(comp);
+            for (auto e : ev) if (e) cudaEventDestroy(e);
+            if (copy) cudaStreamDestroy(copy);
+        }
+    } r;
+    r.comp = p->stream;
+    CUDA_TRY(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+    r.ev.assign((size_t)(2 * K), nullptr);
+    for (auto& e : r.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaStream_t sc = r.comp, sx = r.copy;
+
+    CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), sc));
+    CUDA_TRY(cudaMemsetAsync(queues.p, 0, sizeof(int32_t) * K, sc));
+    {
+        const int grid = (int)std::max<long long>(1, std::min<long long>((n_rows + 255) / 256, (long long)m->dev.sms * 8));
+        if (p->ra.acc_in_smem)
+            prepare_group_ids_kernel<uint16_t><<<grid, 256, 0, sc>>>(p->gid.p, n_rows, (int32_t)p->G, reinterpret_cast<uint16_t*>(p->gidc.p));
+        else
+            prepare_group_ids_kernel<uint32_t><<<grid, 256, 0, sc>>>(p->gid.p, n_rows, (int32_t)p->G, reinterpret_cast<uint32_t*>(p->gidc.p));
+        CUDA_TRY(cudaGetLastError());
+    }
+    for (int k = 0; k < K; ++k) {
+        const long long c0 = cb[k], c1 = cb[k + 1];
+        const long long p0 = indptr[c0], nk = indptr[c1] - p0;
+        cudaEvent_t copied = r.ev[2 * k], narrowed = r.ev[2 * k + 1];
+        if (k >= 2) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (k - 2) + 1], 0));  // staging buffer free
+        if (nk) {
+            CUDA_TRY(cudaMemcpyAsync(m->data.p + p0 * vs, static_cast<const unsigned char*>(data) + p0 * vs,
+                                     (size_t)nk * vs, cudaMemcpyHostToDevice, sx));
+            CUDA_TRY(cudaMemcpyAsync(stage[k & 1].p, indices + p0, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, sx));
+        }
+        CUDA_TRY(cudaEventRecord(copied, sx));
+        CUDA_TRY(cudaStreamWaitEvent(sc, copied, 0));
+        if (nk) {
+            narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sc>>>(
+                stage[k & 1].p, m->rows.p + p0, nk, n_rows);
+            CUDA_TRY(cudaGetLastError());
+        }
+        CUDA_TRY(cudaEventRecord(narrowed, sc));
+        TRY(dispatch_dtype<KeyRangeLaunch>(dtype, (const void*)m->data.p, (const int64_t*)(m->indptr.p + c0), c1 - c0,
+                                           m->col_kmin.p + c0, m->col_kmax.p + c0, m->col_has_zero.p + c0, nk,
+                                           m->dev.sms, sc));
+        RankArgs ra = p->ra;
+        ra.order = p->order.p + c0;
+        ra.n_order = (int32_t)(c1 - c0);
+        ra.queue = queues.p + k;
+        ra.single_gene = -1;
+        TRY(rank_status(rank_launch(dtype, ra, p->rank_grid, p->rank_smem, sc), "rank kernel launch"));
+        PArgs pa{};
+        pa.U1 = p->U1.p;
+        pa.P = p->P.p;
+        pa.n = T * (c1 - c0);
+        pa.n_cols = (int32_t)C;
+        pa.col_lo = (int32_t)c0;
+        pa.col_w = (int32_t)(c1 - c0);
+        pa.U1_out = direct ? U1_out : nullptr;
+        pa.P_out = direct ? P_out : nullptr;
+        pa.group_rows = p->d_group_rows.p;
+        pa.n1g = p->n1.p;
+        pa.n2t = p->n2.p;
+        pa.zero_handling = opt->zero_handling;
+        pa.alternative = opt->alternative;
+        pa.cc = opt->use_continuity ? 0.5 : 0.0;
+        if (direct && k == 0) {
+            CUDA_TRY(cudaLaunchHostFunc(sc, [](void* f) {
+                const auto* done = static_cast<const std::atomic<int>*>(f);
+                while (!done->load(std::memory_order_acquire)) std::this_thread::yield();
+            }, &touched));
+        }
+        if (pa.n) {
+            const int grid = (int)std::min<long long>((pa.n + 255) / 256, (long long)m->dev.sms * 8);
+            mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, sc>>>(pa);
+            CUDA_TRY(cudaGetLastError());
+        }
+    }
+    CUDA_TRY(cudaStreamSynchronize(sc));
+    TRY(check_device_errors(p.get()));
+    if (!direct) TRY(hpdex_plan_download(p.get(), U1_out, P_out));
+    return HPDEX_OK;
+}
+
+}  // namespace
 
 // =======================================================================================
 // No-allocation entry point.
@@ -865,18 +1074,6 @@ __global__ void noalloc_prepare_kernel(const int32_t* gid, long long n_rows, int
     if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_col, mx);
 }
 
-template <class V>
-struct NoAllocKeyRange {
-    static int run(const void* data, const int64_t* indptr, int32_t n_cols, unsigned long long* kmin,
-                   unsigned long long* kmax, unsigned char* hz, cudaStream_t s) {
-        const int threads = 256, wpb = threads / 32;
-        const int grid = (int)std::max<long long>(1, std::min<long long>((n_cols + wpb - 1) / wpb, 65535));
-        column_key_range_kernel<V><<<grid, threads, 0, s>>>(reinterpret_cast<const V*>(data), indptr,
-                                                           n_cols, kmin, kmax, hz);
-        CUDA_TRY(cudaGetLastError());
-        return HPDEX_OK;
-    }
-};
 }  // namespace
 
 extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, const int32_t* d_rows,
@@ -922,7 +1119,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     int32_t* order = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * std::max<long long>(C, 1)));
     unsigned long long* kmin = reinterpret_cast<unsigned long long*>(take(8 * std::max<long long>(C, 1)));
     unsigned long long* kmax = reinterpret_cast<unsigned long long*>(take(8 * std::max<long long>(C, 1)));
-    unsigned char* has_zero = take(std::max<long long>(C, 1));
+    uint32_t* has_zero = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * std::max<long long>(C, 1)));
     uint32_t* n1 = nullptr;
     uint32_t* n2 = nullptr;
     if (zh == HPDEX_ZERO_NONE) {
@@ -997,7 +1194,8 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
         CUDA_TRY(cudaGetLastError());
     }
 
-    TRY(dispatch_dtype<NoAllocKeyRange>(dtype, d_data, d_indptr, (int32_t)C, kmin, kmax, has_zero, s));
+    TRY(dispatch_dtype<KeyRangeLaunch>(dtype, d_data, d_indptr, C, kmin, kmax, has_zero, (long long)longest * C,
+                                       nd->info.sms, s));
     RankArgs a{};
     a.data = d_data;
     a.rows = d_rows;
@@ -1007,6 +1205,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     a.col_has_zero = has_zero;
     a.n_rows = n_rows;
     a.n_cols = (int32_t)C;
+    a.n_order = (int32_t)C;
     a.G = G;
     a.group_of_row = gidc;
     a.order = order;
@@ -1039,6 +1238,8 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     pa.P = d_P;
     pa.n = T * C;
     pa.n_cols = (int32_t)C;
+    pa.col_lo = 0;
+    pa.col_w = (int32_t)C;
     pa.group_rows = group_rows;
     pa.n1g = n1;
     pa.n2t = n2;

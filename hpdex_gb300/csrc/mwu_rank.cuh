@@ -57,13 +57,14 @@ struct RankArgs {
     const int64_t* indptr;     // [n_cols + 1]
     const unsigned long long* col_kmin;  // per column min / max key of finite nonzero values
     const unsigned long long* col_kmax;  //   (kmin > kmax: none)
-    const unsigned char* col_has_zero;   // per column: stores an explicit finite zero
+    const uint32_t* col_has_zero;        // per column: stores an explicit finite zero
     int64_t n_rows;
     int32_t n_cols;
+    int32_t n_order;           // genes in `order` (all columns, or one chunk of them)
     int32_t G;                 // n_targets + 1
     const void* group_of_row;  // [n_rows] group of each row in the kernel's group type
                                // (GroupType below), all ones for rows in no group
-    const int32_t* order;      // genes in processing order [n_cols]
+    const int32_t* order;      // genes in processing order [n_order]
     int32_t* queue;            // work counter (batched form)
     int32_t single_gene;       // >= 0: plain form, this gene only
     int32_t zero_handling;
@@ -654,7 +655,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 c = first ? a.single_gene : -1;
             } else {
                 const int gi = atomicAdd(a.queue, 1);
-                c = gi < a.n_cols ? a.order[gi] : -1;
+                c = gi < a.n_order ? a.order[gi] : -1;
             }
             s_gene = c;
             s_tref = 0ull;
@@ -906,32 +907,63 @@ __global__ void prepare_group_ids_kernel(const int32_t* gid, long long n_rows, i
 }
 
 // Per-column key range of finite nonzero values and whether an explicit finite zero is
-// stored; computed once when a matrix becomes resident (one warp per column).
+// stored, for columns [0, n_cols) of `indptr` (entry positions into `data`). Entry-parallel:
+// a warp takes runs of 32 * kRangePer consecutive entries, lane l the kRangePer entries from
+// l * kRangePer; a lane folds the entries of one column at a time and publishes a column with
+// 64-bit atomics when it leaves it (a warp whose lanes all end in one column combines them
+// first). kmin / kmax / has_zero must hold all ones / 0 / 0 on entry.
+constexpr int kRangePer = 16;
 template <class V>
 __global__ void column_key_range_kernel(const V* data, const int64_t* indptr, int32_t n_cols,
                                         unsigned long long* kmin, unsigned long long* kmax,
-                                        unsigned char* has_zero) {
+                                        uint32_t* has_zero) {
     using K = typename Val<V>::Key;
+    if (n_cols <= 0) return;
+    const long long eb = indptr[0], ee = indptr[n_cols];
+    const long long span = 32ll * kRangePer;
+    const long long runs = (ee - eb + span - 1) / span;
     const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    for (int c = blockIdx.x * wpb + (threadIdx.x >> 5); c < n_cols; c += gridDim.x * wpb) {
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < runs; r += nw) {
+        const long long s0 = eb + r * span + (long long)lane * kRangePer;
+        const long long s1 = s0 + kRangePer < ee ? s0 + kRangePer : ee;
+        int col = -1;
         K lo = ~K(0), hi = K(0);
         bool z = false;
-        for (long long p = indptr[c] + lane; p < indptr[c + 1]; p += 32) {
-            const V v = data[p];
-            if (!Val<V>::finite(v)) continue;
-            if (Val<V>::zero(v)) { z = true; continue; }
-            const K k = Val<V>::key(v);
-            lo = k < lo ? k : lo;
-            hi = k > hi ? k : hi;
+        auto publish = [&](int c) {
+            if (lo <= hi) {
+                atomicMin(&kmin[c], (unsigned long long)lo);
+                atomicMax(&kmax[c], (unsigned long long)hi);
+            }
+            if (z) atomicOr(&has_zero[c], 1u);
+            lo = ~K(0); hi = K(0); z = false;
+        };
+        if (s0 < ee) {
+            int a = 0, b = n_cols - 1;  // the column holding s0: last c with indptr[c] <= s0
+            while (a < b) {
+                const int mid = (a + b + 1) >> 1;
+                if (indptr[mid] <= s0) a = mid; else b = mid - 1;
+            }
+            col = a;
+            long long cend = indptr[col + 1];
+            for (long long e = s0; e < s1; ++e) {
+                while (e >= cend) { publish(col); ++col; cend = indptr[col + 1]; }
+                const V v = data[e];
+                if (!Val<V>::finite(v)) continue;
+                if (Val<V>::zero(v)) { z = true; continue; }
+                const K k = Val<V>::key(v);
+                lo = k < lo ? k : lo;
+                hi = k > hi ? k : hi;
+            }
         }
-        lo = warp_min(lo);
-        hi = warp_max(hi);
-        z = __any_sync(0xffffffffu, z);
-        if (lane == 0) {
-            kmin[c] = lo;
-            kmax[c] = hi;
-            has_zero[c] = z ? 1 : 0;
+        const int c0 = __shfl_sync(0xffffffffu, col, 0);
+        if (__all_sync(0xffffffffu, col == c0 || col < 0)) {
+            lo = warp_min(lo);
+            hi = warp_max(hi);
+            z = __any_sync(0xffffffffu, z);
+            if (lane == 0 && c0 >= 0) publish(c0);
+        } else if (col >= 0) {
+            publish(col);
         }
     }
 }

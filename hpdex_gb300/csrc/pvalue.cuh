@@ -22,9 +22,12 @@ namespace hpdex {
 
 struct PArgs {
     const double* U1;
-    double* P;                 // holds the (masked) tie sum on entry, P on exit
-    long long n;               // T * n_cols
+    double* P;                 // holds the (masked) tie sum on entry; P on exit unless P_out
+    long long n;               // T * col_w: the tests of columns [col_lo, col_lo + col_w)
     int32_t n_cols;
+    int32_t col_lo, col_w;
+    double* U1_out;            // optional: U1 and P written here instead (same [T][n_cols]
+    double* P_out;             //   layout; may be host memory the device can access)
     const long long* group_rows;
     const uint32_t* n1g;       // zero_handling = none: per gene
     const uint32_t* n2t;       // zero_handling = none: per test
@@ -33,12 +36,17 @@ struct PArgs {
     double cc;
 };
 
-__device__ __forceinline__ void test_sizes(const PArgs& a, long long i, double& n1, double& n2) {
-    const int t = (int)(i / a.n_cols);
-    const int c = (int)(i - (long long)t * a.n_cols);
+// test i of the column range -> its target t and column c, at idx = t * n_cols + c
+__device__ __forceinline__ long long test_index(const PArgs& a, long long i, int& t, int& c) {
+    t = (int)(i / a.col_w);
+    c = a.col_lo + (int)(i - (long long)t * a.col_w);
+    return (long long)t * a.n_cols + c;
+}
+__device__ __forceinline__ void test_sizes(const PArgs& a, int t, int c, long long idx, double& n1,
+                                           double& n2) {
     if (a.zero_handling == ZH_NONE) {
         n1 = (double)a.n1g[c];
-        n2 = (double)a.n2t[i];
+        n2 = (double)a.n2t[idx];
     } else {
         n1 = (double)a.group_rows[0];
         n2 = (double)a.group_rows[t + 1];
@@ -81,9 +89,18 @@ __device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, 
 __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        int t, c;
+        const long long idx = test_index(a, i, t, c);
         double n1, n2;
-        test_sizes(a, i, n1, n2);
-        a.P[i] = p_asymptotic(a.U1[i], n1, n2, a.P[i], a.cc, a.alternative);
+        test_sizes(a, t, c, idx, n1, n2);
+        const double u1 = a.U1[idx];
+        const double p = p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative);
+        if (a.P_out) {
+            a.U1_out[idx] = u1;
+            a.P_out[idx] = p;
+        } else {
+            a.P[idx] = p;
+        }
     }
 }
 
