@@ -11,7 +11,9 @@ One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
           CUDA events recorded inside the graph on the launching stream.
   e2e   : tests/s through the reference-shaped public call kernel.mannwhitneyu with host
           numpy arrays in and out (H2D of values, int64 row ids, column pointers and
-          group ids; D2H of U1 and P), wall clock.
+          group ids; D2H of U1 and P), wall clock. The call uploads the matrix in column
+          chunks and ranks chunk k while chunk k+1 is in flight; on coherent-memory systems
+          the p-value kernel writes U1 and P straight into the output arrays.
   plain : the same call in the plain form (one launch per gene, no graph, no queue).
 The inputs (1.17 GB resident) exceed the 129 MB L2, so no flush is needed between steps.
 

@@ -18,8 +18,11 @@ def __getattr__(name):
     if name in ("ResidentMatrix", "Plan"):
         from . import resident
         return getattr(resident, name)
+    if name == "release_cached_memory":
+        from ._lib import release_cached_memory
+        return release_cached_memory
     raise AttributeError(name)
 
 
 __all__ = ["mannwhitneyu", "group_mean", "parallel_differential_expression",
-           "differential_expression", "ResidentMatrix", "Plan"]
+           "differential_expression", "ResidentMatrix", "Plan", "release_cached_memory"]

@@ -41,6 +41,7 @@ EXPORTS = {
     "hpdex_mwu_options_default": (None, [ctypes.POINTER(MwuOptions)]),
     "hpdex_last_error": (ctypes.c_char_p, []),
     "hpdex_device_count": (ctypes.c_int, []),
+    "hpdex_release_cached_memory": (ctypes.c_int, []),
     "hpdex_mannwhitneyu": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
@@ -104,3 +105,8 @@ def check(status: int) -> None:
 
 def device_count() -> int:
     return int(lib().hpdex_device_count())
+
+
+def release_cached_memory() -> None:
+    """Return the device memory that finished calls keep cached for reuse to the driver."""
+    check(lib().hpdex_release_cached_memory())

@@ -114,21 +114,102 @@ __global__ void narrow_rows_kernel(const long long* in, int32_t* out, long long 
     }
 }
 
+// Device memory cache. A released block stays reserved for its device and is handed out
+// again to a request of at most its size and at least half of it, so repeated calls (the
+// one-shot call allocates a matrix, a plan and their scratch every time) skip cudaMalloc and
+// cudaFree. Every entry point returns with its device work complete, so a released block is
+// idle. hpdex_release_cached_memory() returns the cached blocks to the driver; an allocation
+// that fails does the same for its device and retries once.
+class MemCache {
+    struct Dev {
+        std::multimap<size_t, void*> idle;
+        size_t idle_bytes = 0;
+    };
+    std::mutex mu_;
+    std::map<int, Dev> dev_;
+    std::map<void*, std::pair<int, size_t>> live_;  // pointer -> device, block size
+
+    static size_t round(size_t b) {
+        const size_t g = b >= (size_t(1) << 20) ? (size_t(1) << 20) : 512;
+        return (b + g - 1) / g * g;
+    }
+    void drop_idle(int dev) {  // caller holds mu_
+        auto& d = dev_[dev];
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (cur != dev) cudaSetDevice(dev);
+        for (auto& kv : d.idle) cudaFree(kv.second);
+        if (cur != dev && cur >= 0) cudaSetDevice(cur);
+        d.idle.clear();
+        d.idle_bytes = 0;
+    }
+
+  public:
+    cudaError_t get(void** out, size_t bytes) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        const size_t want = round(bytes);
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            auto& d = dev_[dev];
+            auto it = d.idle.lower_bound(want);
+            if (it != d.idle.end() && it->first / 2 <= want) {
+                *out = it->second;
+                live_[*out] = {dev, it->first};
+                d.idle_bytes -= it->first;
+                d.idle.erase(it);
+                return cudaSuccess;
+            }
+        }
+        e = cudaMalloc(out, want);
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            std::lock_guard<std::mutex> lock(mu_);
+            drop_idle(dev);
+            e = cudaMalloc(out, want);
+        }
+        if (e != cudaSuccess) { *out = nullptr; return e; }
+        std::lock_guard<std::mutex> lock(mu_);
+        live_[*out] = {dev, want};
+        return cudaSuccess;
+    }
+    void put(void* p) {
+        if (!p) return;
+        std::lock_guard<std::mutex> lock(mu_);
+        auto it = live_.find(p);
+        if (it == live_.end()) { cudaFree(p); return; }
+        auto& d = dev_[it->second.first];
+        d.idle.insert({it->second.second, p});
+        d.idle_bytes += it->second.second;
+        live_.erase(it);
+    }
+    void release_all() {
+        std::lock_guard<std::mutex> lock(mu_);
+        for (auto& kv : dev_) drop_idle(kv.first);
+    }
+};
+MemCache& mem_cache() {
+    static MemCache* c = new MemCache();  // never destroyed: blocks are released to the driver at exit
+    return *c;
+}
+
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
-    ~DevBuf() { if (p) cudaFree(p); }
+    ~DevBuf() { mem_cache().put(p); }
     int alloc(size_t count) {
-        if (p) { cudaFree(p); p = nullptr; }
+        if (p) { mem_cache().put(p); p = nullptr; }
         n = count;
         if (count == 0) return HPDEX_OK;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        void* q = nullptr;
+        cudaError_t e = mem_cache().get(&q, count * sizeof(T));
         if (e != cudaSuccess) {
-            p = nullptr;
-            return fail(HPDEX_ERR_CUDA, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T),
+            return fail(HPDEX_ERR_CUDA, "device allocation of %zu bytes failed: %s", count * sizeof(T),
                         cudaGetErrorString(e));
         }
+        p = static_cast<T*>(q);
         return HPDEX_OK;
     }
 };
@@ -547,6 +628,8 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
 int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
                       int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
                       int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out);
+int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
+                const hpdex_mwu_options* opt, hpdex_plan** out, bool lpt_order);
 
 }  // namespace
 
@@ -567,6 +650,11 @@ void hpdex_mwu_options_default(hpdex_mwu_options* o) {
 }
 
 const char* hpdex_last_error(void) { return g_last_error.c_str(); }
+
+int hpdex_release_cached_memory(void) {
+    mem_cache().release_all();
+    return HPDEX_OK;
+}
 
 int hpdex_device_count(void) {
     int n = 0;
@@ -615,6 +703,16 @@ int hpdex_matrix_info(const hpdex_matrix* m, int64_t* n_rows, int64_t* n_cols, i
 
 int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
                       const hpdex_mwu_options* opt, hpdex_plan** out) {
+    return plan_create(m, group_id, n_targets, opt, out, true);
+}
+
+}  // extern "C"
+
+namespace {
+// lpt_order: fill the work queue's gene order (longest first) here; the pipelined one-shot
+// call writes its own per-chunk order instead
+int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
+                const hpdex_mwu_options* opt, hpdex_plan** out, bool lpt_order) {
     if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
     *out = nullptr;
     if (!m || !opt) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix or options");
@@ -650,13 +748,15 @@ int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_target
     TRY(p->d_group_rows.alloc((size_t)G));
     CUDA_TRY(cudaMemcpy(p->d_group_rows.p, p->group_rows.data(), sizeof(long long) * G, cudaMemcpyHostToDevice));
     // longest genes first: the work queue hands them out before the short tail
-    std::vector<int32_t> order((size_t)C);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
-        return m->col_nnz[(size_t)a] > m->col_nnz[(size_t)b];
-    });
     TRY(p->order.alloc(std::max<long long>(C, 1)));
-    if (C) CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
+    if (lpt_order && C) {
+        std::vector<int32_t> order((size_t)C);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return m->col_nnz[(size_t)a] > m->col_nnz[(size_t)b];
+        });
+        CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
+    }
     TRY(p->queue.alloc(1));
     TRY(p->err.alloc(kErrWords));
     const size_t n = (size_t)(p->T * C);
@@ -670,6 +770,10 @@ int hpdex_plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_target
     *out = p.release();
     return HPDEX_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int hpdex_plan_destroy(hpdex_plan* p) {
     delete p;
@@ -836,7 +940,10 @@ int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
 // =======================================================================================
 namespace {
 
-constexpr int kPipelineChunks = 8;
+// relative chunk sizes; the compute left after the last copy is about the longest gene of
+// the last chunk, so the last chunk is not made smaller than that needs
+constexpr int kPipelineWeights[] = {4, 4, 4, 4, 4, 4, 4, 3};
+constexpr int kPipelineChunks = sizeof(kPipelineWeights) / sizeof(int);
 
 int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
                       int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
@@ -867,15 +974,18 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
     }
     hpdex_plan* praw = nullptr;
-    TRY(hpdex_plan_create(m.get(), group_id, n_targets, opt, &praw));
+    TRY(plan_create(m.get(), group_id, n_targets, opt, &praw, false));
     std::unique_ptr<hpdex_plan> p(praw);
     const long long T = p->T;
     if (C == 0) return HPDEX_OK;
 
     // chunks of about nnz / kPipelineChunks entries (whole columns)
     std::vector<long long> cb{0};
+    int wsum = 0, wacc = 0;
+    for (int w : kPipelineWeights) wsum += w;
     for (int k = 1; k < kPipelineChunks; ++k) {
-        const long long target = nnz / kPipelineChunks * k;
+        wacc += kPipelineWeights[k - 1];
+        const long long target = (long long)((double)nnz * wacc / wsum);
         const long long c = std::lower_bound(indptr, indptr + C + 1, target) - indptr;
         if (c > cb.back() && c < C) cb.push_back(c);
     }

@@ -88,6 +88,10 @@ const char* hpdex_last_error(void);
 /* Number of visible CUDA devices (0 when none); never fails. */
 int hpdex_device_count(void);
 
+/* Device memory of destroyed matrices, plans and finished one-shot calls stays cached for
+ * reuse by later calls (no cudaMalloc/cudaFree per call); this returns it to the driver. */
+int hpdex_release_cached_memory(void);
+
 /* ---- one-shot calls (reference semantics; host pointers in and out) ---- */
 
 /* kernel.mannwhitneyu. threads is accepted for signature parity and only affects host-side
