@@ -15,6 +15,11 @@ One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
           chunks and ranks chunk k while chunk k+1 is in flight; on coherent-memory systems
           the p-value kernel writes U1 and P straight into the output arrays.
   plain : the same call in the plain form (one launch per gene, no graph, no queue).
+  serving: the serving loop (hpdex_gb300.serving) over three resident matrices (the
+          200k x 8k screen, a 50k x 2k log1p-CP10k matrix and a 50k x 2k integer-count
+          matrix), Poisson arrivals of random groupings (reference 1k-50k cells, 1-200
+          targets of 20-5,000 cells), p50/p99 latency and tests/s, coalesced launches
+          (max_batch=16) against per-query launches (max_batch=1), at two arrival rates.
 The inputs (1.17 GB resident) exceed the 129 MB L2, so no flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference backend (oracle/, OpenMP over all
@@ -176,6 +181,33 @@ def run_reference(args, rank, world):
     return 0
 
 
+def serving_leg(M, w, queries=150, rates=(300.0, 1500.0)):
+    """Serving loop on the resident screen plus two 50k x 2k matrices (see module doc)."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix
+    from hpdex_gb300.serving import Server, poisson_run
+    b = synthetic.perturb_screen(seed=3, n_rows=50_000, n_cols=2_000, n_targets=50, ref_size=5_000)
+    c = synthetic.umi_counts(seed=4, n_rows=50_000, n_cols=2_000)
+    mats = [M, ResidentMatrix(b.data, b.indices, b.indptr, b.n_rows),
+            ResidentMatrix(c.data, c.indices, c.indptr, c.n_rows)]
+    rows = {0: w.n_rows, 1: b.n_rows, 2: c.n_rows}
+    runs = []
+    for mode, mb in (("coalesced", 16), ("per_query", 1)):
+        for rate in rates:
+            with Server(workspace_bytes=32 << 30, max_batch=mb) as srv:
+                ids = [srv.add_matrix(m) for m in mats]
+                poisson_run(srv, ids, rows, rate_qps=rate, n_queries=20, seed=1)  # warm-up
+                r = poisson_run(srv, ids, rows, rate_qps=rate, n_queries=queries, seed=2)
+            runs.append({"mode": mode, "max_batch": mb, "rate_qps": rate,
+                         "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "mean_ms": r["mean_ms"],
+                         "tests_per_s": r["tests_per_s"], "launches": r["batches"],
+                         "gpu_busy_ms": r["busy_ms"]})
+    return {"matrices": "200000x8000 screen (1.47e8 nnz), 50000x2000 log1p-CP10k, "
+                        "50000x2000 integer counts; all resident float32",
+            "queries_per_run": queries, "arrival": "Poisson", "runs": runs,
+            "note": "latency = submit to results in host memory; tests/s over the run's wall time"}
+
+
 def run_ours(args, rank, world):
     from hpdex_gb300 import _lib
     from hpdex_gb300.backend.bin import kernel
@@ -248,6 +280,8 @@ def run_ours(args, rank, world):
     e2e_wall = (time.perf_counter() - te) / e2e_steps
     same = same and bool(np.array_equal(U1e, U1) and np.array_equal(Pe, P))
 
+    serving = serving_leg(M, w) if not args.no_serving else None
+
     hbm, peak_kind = peaks()
     B = algorithmic_bytes(w)
     rank_avg = statistics.mean(rank_ms) / 1e3
@@ -273,6 +307,7 @@ def run_ours(args, rank, world):
                   "batched_speedup": (tests / elapsed_dev * args.steps) / (tests / (ptot / 1e3)),
                   "results_identical": same},
         "kernels_ms": {"rank": statistics.mean(rank_ms), "pvalue": statistics.mean(p_ms)},
+        "serving": serving,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
                      "kernel": "mwu_rank_kernel", "algorithmic_bytes": B,
@@ -298,6 +333,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-genes", type=int, default=800)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched form only (no plain form, e2e or CPU legs); for ncu")
     args = ap.parse_args()

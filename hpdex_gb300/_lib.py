@@ -19,7 +19,8 @@ DTYPE_CODES = {
     "int64": 6, "uint64": 7, "float32": 8, "float64": 9,
 }
 
-HPDEX_OK, HPDEX_ERR_RUNTIME, HPDEX_ERR_ARGUMENT, HPDEX_ERR_CUDA, HPDEX_ERR_UNSUPPORTED = range(5)
+(HPDEX_OK, HPDEX_ERR_RUNTIME, HPDEX_ERR_ARGUMENT, HPDEX_ERR_CUDA, HPDEX_ERR_UNSUPPORTED,
+ HPDEX_ERR_TIMEOUT) = range(6)
 
 
 class MwuOptions(ctypes.Structure):
@@ -70,6 +71,20 @@ EXPORTS = {
                                                   ctypes.c_void_p, ctypes.c_int64,
                                                   ctypes.POINTER(MwuOptions), ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p]),
+    "hpdex_server_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_server_add_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_int32)]),
+    "hpdex_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.POINTER(MwuOptions),
+                                           ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_int64)]),
+    "hpdex_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+                                         ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 

@@ -8,6 +8,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -246,6 +249,8 @@ struct hpdex_plan {
     DevBuf<unsigned char> dk, ek;
     DevBuf<unsigned char> dg, eg;
     DevBuf<unsigned char> gidc;  // group of each row in the rank kernel's group type
+    RankTask task{};             // this plan as a rank-kernel task (host copy)
+    DevBuf<RankTask> d_task;
     DevBuf<unsigned char> acc;
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
@@ -377,81 +382,118 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
     return HPDEX_OK;
 }
 
+// The rank-kernel task of a plan: its matrix, grouping and output buffers.
+RankTask task_of(const hpdex_matrix* m, const hpdex_plan* p) {
+    RankTask t{};
+    t.data = m->data.p;
+    t.rows = m->rows.p;
+    t.indptr = m->indptr.p;
+    t.col_kmin = m->col_kmin.p;
+    t.col_kmax = m->col_kmax.p;
+    t.col_has_zero = m->col_has_zero.p;
+    t.n_rows = m->n_rows;
+    t.n_cols = (int32_t)m->n_cols;
+    t.G = (int32_t)p->G;
+    t.group_of_row = p->gidc.p;
+    t.zero_handling = p->opt.zero_handling;
+    t.tie_correction = p->opt.tie_correction;
+    t.group_rows = p->d_group_rows.p;
+    t.U1 = p->U1.p;
+    t.tie = p->P.p;
+    t.n1 = p->n1.p;
+    t.n2 = p->n2.p;
+    t.err = p->err.p;
+    return t;
+}
+
 // Rank-kernel layout for this plan: one 1024-thread CTA per SM; the bucket table takes
 // 2^13 entries, then the per-target accumulators, the run counters of as many warps as fit
 // (at least 4, else in global memory), and the rest holds a gene's elements when it fits.
-int configure_rank(hpdex_plan* p) {
-    const hpdex_matrix* m = p->m;
-    const int kb = key_bytes(m->dtype);
-    const int G = (int)p->G;
-    const int nbl = 13;
-    const int tie_warps = kRankThreads / 32;  // every warp resolves buckets
-    const size_t budget = std::min(m->dev.smem_per_sm - m->dev.smem_reserved, m->dev.smem_optin) - 2048;
+// Shared-memory layout, grid and scratch sizes of a rank launch for value type `dtype`,
+// layout G and longest column `max_col`.
+struct RankLayout {
+    int nbl = 13, tie_warps = kRankThreads / 32, acc_in = 1, cap = 0, grid = 0, kb = 4, gb = 2;
+    size_t smem = 0;
+    long long slice = 0;
+    bool need_slab_scratch = false;  // some column exceeds the shared-memory capacity
+    size_t dk_bytes() const { return (size_t)grid * slice * kb; }
+    size_t dg_bytes() const { return (size_t)grid * slice * gb; }
+    size_t acc_bytes(int G) const { return acc_in ? 0 : (size_t)grid * 24 * G; }
+    size_t cnt_words(int G) const { return (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G); }
+};
+
+int rank_layout(const DeviceInfo& dev, int dtype, int G, long long max_col, RankLayout* out) {
+    RankLayout r;
+    r.kb = key_bytes(dtype);
+    const size_t budget = std::min(dev.smem_per_sm - dev.smem_reserved, dev.smem_optin) - 2048;
     // accumulators and run counters live together: both in shared memory, or both global
-    int acc_in = 1, cnt_in = 1;
-    RankSmem L(nbl, G, tie_warps, acc_in, cnt_in, 0, kb);
-    if (L.total + 16384 > budget) { acc_in = cnt_in = 0; L = RankSmem(nbl, G, tie_warps, 0, 0, 0, kb); }
+    RankSmem L(r.nbl, G, r.tie_warps, 1, 1, 0, r.kb);
+    if (L.total + 16384 > budget) { r.acc_in = 0; L = RankSmem(r.nbl, G, r.tie_warps, 0, 0, 0, r.kb); }
     if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
     const size_t left = budget - L.total;
-    const int gb = group_bytes(acc_in);
-    int cap = (int)std::min<size_t>(left / (kb + gb + 1), (size_t)1 << 30);  // + big-list entry share
-    cap = std::max(0, cap - 8) & ~7;
-    L = RankSmem(nbl, G, tie_warps, acc_in, cnt_in, cap, kb);
-    p->rank_smem = L.total;
-
+    r.gb = group_bytes(r.acc_in);
+    r.cap = (int)std::min<size_t>(left / (r.kb + r.gb + 1), (size_t)1 << 30);  // + big-list entry share
+    r.cap = std::max(0, r.cap - 8) & ~7;
+    L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.acc_in, r.cap, r.kb);
+    r.smem = L.total;
     int blocks = 0;
-    TRY(rank_status(rank_occupancy(m->dtype, p->rank_smem, m->dev.smem_optin, acc_in, &blocks), "rank kernel set-up"));
-    if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM (smem %zu)", p->rank_smem);
-    p->rank_grid = m->dev.sms * blocks;
+    TRY(rank_status(rank_occupancy(dtype, r.smem, dev.smem_optin, r.acc_in, &blocks), "rank kernel set-up"));
+    if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM (smem %zu)", r.smem);
+    r.grid = dev.sms * blocks;
+    // whole 128-byte lines per CTA slice (vector access, L2 discards)
+    r.slice = rank_slice(max_col);
+    r.need_slab_scratch = (long long)r.cap < max_col;
+    *out = r;
+    return HPDEX_OK;
+}
 
-    // whole 128-byte lines per CTA slice (vector access, bulk copies, L2 discards)
-    const long long slice = rank_slice(m->max_col_nnz);
-    const size_t nctas = (size_t)p->rank_grid;
-    TRY(p->dk.alloc(nctas * slice * kb));
-    TRY(p->dg.alloc(nctas * slice * gb));
-    if ((long long)cap < m->max_col_nnz) {
-        TRY(p->ek.alloc(nctas * slice * kb));
-        TRY(p->eg.alloc(nctas * slice * gb));
-    }
-    TRY(p->gidc.alloc((size_t)std::max<long long>(m->n_rows, 1) * gb));
-    if (!acc_in) TRY(p->acc.alloc(nctas * 24 * (size_t)G));
-    TRY(p->cnt.alloc(nctas * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
-
-    RankArgs& a = p->ra;
-    a.data = m->data.p;
-    a.rows = m->rows.p;
-    a.indptr = m->indptr.p;
-    a.col_kmin = m->col_kmin.p;
-    a.col_kmax = m->col_kmax.p;
-    a.col_has_zero = m->col_has_zero.p;
-    a.n_rows = m->n_rows;
-    a.n_cols = (int32_t)m->n_cols;
-    a.n_order = (int32_t)m->n_cols;
+// Fills the launch-wide fields of RankArgs (layout and scratch) from a layout.
+void set_layout_args(RankArgs& a, const RankLayout& r, int G, void* dk, void* dg, void* ek, void* eg,
+                     unsigned char* acc, uint32_t* cnt) {
     a.G = G;
-    a.group_of_row = p->gidc.p;
+    a.dk_global = dk;
+    a.dg_global = dg;
+    a.ek_global = ek;
+    a.eg_global = eg;
+    a.slice = r.slice;
+    a.acc_global = acc;
+    a.cnt_global = cnt;
+    a.nb_max_log2 = r.nbl;
+    a.elem_smem_cap = r.cap;
+    a.acc_in_smem = r.acc_in;
+    a.cnt_in_smem = r.acc_in;
+    a.tie_warps = r.tie_warps;
+}
+
+int configure_rank(hpdex_plan* p) {
+    const hpdex_matrix* m = p->m;
+    const int G = (int)p->G;
+    RankLayout r;
+    TRY(rank_layout(m->dev, m->dtype, G, m->max_col_nnz, &r));
+    p->rank_smem = r.smem;
+    p->rank_grid = r.grid;
+    TRY(p->dk.alloc(r.dk_bytes()));
+    TRY(p->dg.alloc(r.dg_bytes()));
+    if (r.need_slab_scratch) {
+        TRY(p->ek.alloc(r.dk_bytes()));
+        TRY(p->eg.alloc(r.dg_bytes()));
+    }
+    TRY(p->gidc.alloc((size_t)std::max<long long>(m->n_rows, 1) * r.gb));
+    if (!r.acc_in) TRY(p->acc.alloc(r.acc_bytes(G)));
+    TRY(p->cnt.alloc(r.cnt_words(G)));
+
+    RankTask& t = p->task;
+    t = task_of(m, p);
+    TRY(p->d_task.alloc(1));
+    CUDA_TRY(cudaMemcpy(p->d_task.p, &t, sizeof(RankTask), cudaMemcpyHostToDevice));
+    RankArgs& a = p->ra;
+    a.tasks = p->d_task.p;
     a.order = p->order.p;
+    a.order_task = nullptr;
+    a.n_order = (int32_t)m->n_cols;
     a.queue = p->queue.p;
     a.single_gene = -1;
-    a.zero_handling = p->opt.zero_handling;
-    a.tie_correction = p->opt.tie_correction;
-    a.group_rows = p->d_group_rows.p;
-    a.U1 = p->U1.p;
-    a.tie = p->P.p;
-    a.n1 = p->n1.p;
-    a.n2 = p->n2.p;
-    a.err = p->err.p;
-    a.dk_global = p->dk.p;
-    a.dg_global = p->dg.p;
-    a.ek_global = p->ek.p;
-    a.eg_global = p->eg.p;
-    a.slice = slice;
-    a.acc_global = p->acc.p;
-    a.cnt_global = p->cnt.p;
-    a.nb_max_log2 = nbl;
-    a.elem_smem_cap = cap;
-    a.acc_in_smem = acc_in;
-    a.cnt_in_smem = cnt_in;
-    a.tie_warps = tie_warps;
+    set_layout_args(a, r, G, p->dk.p, p->dg.p, p->ek.p, p->eg.p, p->acc.p, p->cnt.p);
     return HPDEX_OK;
 }
 
@@ -577,21 +619,35 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
     return HPDEX_OK;
 }
 
-int check_device_errors(hpdex_plan* p) {
-    unsigned long long e[kErrWords];
-    CUDA_TRY(cudaMemcpy(e, p->err.p, sizeof e, cudaMemcpyDeviceToHost));
-    const unsigned long long G = (unsigned long long)p->G;
+// The status and message of a run's device error words (reference wording: the lowest
+// (column, group) wins, as in the single-threaded reference).
+int decode_errors(const unsigned long long* e, long long G_, std::string* msg) {
+    const unsigned long long G = (unsigned long long)G_;
+    char buf[256];
     if (e[0] != ~0ull) {
         const unsigned long long c = e[0] / G, g = e[0] % G;
-        if (g == 0) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column %llu", c);
-        return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %llu at column %llu", g, c);
+        if (g == 0) snprintf(buf, sizeof buf, "Sample too small for reference at column %llu", c);
+        else snprintf(buf, sizeof buf, "Sample too small for group %llu at column %llu", g, c);
+        *msg = buf;
+        return HPDEX_ERR_RUNTIME;
     }
     if (e[1] != ~0ull) {
         const unsigned long long c = e[1] / G, g = e[1] % G;
-        return fail(HPDEX_ERR_ARGUMENT,
-                    "column %llu stores more entries for group %llu than the group has rows "
-                    "(duplicate row indices)", c, g);
+        snprintf(buf, sizeof buf,
+                 "column %llu stores more entries for group %llu than the group has rows "
+                 "(duplicate row indices)", c, g);
+        *msg = buf;
+        return HPDEX_ERR_ARGUMENT;
     }
+    return HPDEX_OK;
+}
+
+int check_device_errors(hpdex_plan* p) {
+    unsigned long long e[kErrWords];
+    CUDA_TRY(cudaMemcpy(e, p->err.p, sizeof e, cudaMemcpyDeviceToHost));
+    std::string msg;
+    const int st = decode_errors(e, p->G, &msg);
+    if (st != HPDEX_OK) return fail(st, "%s", msg.c_str());
     return HPDEX_OK;
 }
 
@@ -1114,6 +1170,472 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
 }  // namespace
 
 // =======================================================================================
+// Serving loop.
+//
+// A worker thread turns a stream of DE queries (a grouping over a resident matrix) into
+// batched launches. Admission is in arrival order while the queries' device workspace fits the
+// budget; the admitted queries of one value dtype (up to max_batch) become one launch of the
+// persistent rank kernel with one task per query and one longest-first work queue of
+// (query, gene) items, followed by one p-value kernel per query. Up to two batches are queued
+// on the GPU at once, so the next batch is prepared while the previous one runs, and a query
+// that arrives meanwhile joins the next launch. Completion is tracked per batch with an event;
+// the worker then reads each query's error words, releases its workspace and wakes waiters.
+// =======================================================================================
+namespace {
+
+struct ServerQuery {
+    int64_t id = 0;
+    int matrix = 0;
+    long long T = 0, G = 0;
+    hpdex_mwu_options opt{};
+    std::vector<int32_t> gid;
+    std::vector<long long> group_rows;
+    double* U1_out = nullptr;
+    double* P_out = nullptr;
+    size_t need = 0;  // device workspace bytes while admitted
+    DevBuf<int32_t> d_gid;
+    DevBuf<unsigned char> gidc;
+    DevBuf<long long> d_group_rows;
+    DevBuf<double> U1, P;
+    DevBuf<uint32_t> n1, n2;
+    DevBuf<unsigned long long> err;
+    bool direct = false;  // p-values written straight into the host arrays
+    int status = -1;      // -1 while pending or running
+    std::string error;
+    std::chrono::steady_clock::time_point t_submit, t_done;
+};
+
+struct ServerBatch {
+    std::vector<ServerQuery*> q;
+    DevBuf<RankTask> tasks;
+    DevBuf<int32_t> order, queue;
+    DevBuf<uint16_t> order_task;
+    DevBuf<unsigned char> dk, dg, ek, eg, acc;
+    DevBuf<uint32_t> cnt;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    ~ServerBatch() {
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+    }
+};
+
+}  // namespace
+
+struct hpdex_server {
+    size_t budget = 0;
+    int max_batch = 1;
+    DeviceInfo dev;
+    std::vector<hpdex_matrix*> mats;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<ServerQuery*> pending;
+    std::map<int64_t, std::unique_ptr<ServerQuery>> queries;
+    int64_t next_id = 1;
+    size_t used = 0;
+    bool stop = false;
+    int64_t completed = 0, batches = 0;
+    double busy_ms = 0.0;
+    cudaStream_t stream = nullptr;
+    std::thread worker;
+};
+
+namespace {
+
+// Workspace of one admitted query: outputs, group ids (int32 and kernel type), group sizes,
+// sample sizes under zero_handling=none.
+size_t query_workspace(const hpdex_matrix* m, long long T, long long G, int zh) {
+    const size_t tc = (size_t)(T * m->n_cols);
+    size_t b = 16 * tc + 8 * (size_t)m->n_rows + 8 * (size_t)G + 64;
+    if (zh == HPDEX_ZERO_NONE) b += 4 * tc + 4 * (size_t)m->n_cols;
+    return b;
+}
+
+// Queues one batch on the server stream; on failure the caller fails its queries.
+int server_launch(hpdex_server* S, ServerBatch& b) {
+    cudaStream_t st = S->stream;
+    const hpdex_matrix* m0 = S->mats[(size_t)b.q[0]->matrix];
+    const int dtype = m0->dtype;
+    int GL = 0;
+    long long max_col = 0, items = 0;
+    for (ServerQuery* q : b.q) {
+        const hpdex_matrix* m = S->mats[(size_t)q->matrix];
+        GL = std::max(GL, (int)q->G);
+        max_col = std::max(max_col, m->max_col_nnz);
+        items += m->n_cols;
+    }
+    RankLayout r;
+    TRY(rank_layout(S->dev, dtype, GL, max_col, &r));
+    TRY(b.dk.alloc(r.dk_bytes()));
+    TRY(b.dg.alloc(r.dg_bytes()));
+    if (r.need_slab_scratch) {
+        TRY(b.ek.alloc(r.dk_bytes()));
+        TRY(b.eg.alloc(r.dg_bytes()));
+    }
+    if (!r.acc_in) TRY(b.acc.alloc(r.acc_bytes(GL)));
+    TRY(b.cnt.alloc(r.cnt_words(GL)));
+
+    std::vector<RankTask> tasks(b.q.size());
+    for (size_t i = 0; i < b.q.size(); ++i) {
+        ServerQuery* q = b.q[i];
+        const hpdex_matrix* m = S->mats[(size_t)q->matrix];
+        const long long R = m->n_rows, C = m->n_cols, tc = q->T * C;
+        TRY(q->d_gid.alloc((size_t)std::max<long long>(R, 1)));
+        TRY(q->gidc.alloc((size_t)std::max<long long>(R, 1) * r.gb));
+        TRY(q->d_group_rows.alloc((size_t)q->G));
+        TRY(q->U1.alloc((size_t)std::max<long long>(tc, 1)));
+        TRY(q->P.alloc((size_t)std::max<long long>(tc, 1)));
+        if (q->opt.zero_handling == HPDEX_ZERO_NONE) {
+            TRY(q->n1.alloc((size_t)std::max<long long>(C, 1)));
+            TRY(q->n2.alloc((size_t)std::max<long long>(tc, 1)));
+        }
+        TRY(q->err.alloc(kErrWords));
+        if (R) CUDA_TRY(cudaMemcpyAsync(q->d_gid.p, q->gid.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(q->d_group_rows.p, q->group_rows.data(), sizeof(long long) * q->G, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemsetAsync(q->err.p, 0xff, kErrWords * sizeof(unsigned long long), st));
+        const int grid = (int)std::max<long long>(1, std::min<long long>((R + 255) / 256, (long long)S->dev.sms * 8));
+        if (r.acc_in)
+            prepare_group_ids_kernel<uint16_t><<<grid, 256, 0, st>>>(q->d_gid.p, R, (int32_t)q->G, reinterpret_cast<uint16_t*>(q->gidc.p));
+        else
+            prepare_group_ids_kernel<uint32_t><<<grid, 256, 0, st>>>(q->d_gid.p, R, (int32_t)q->G, reinterpret_cast<uint32_t*>(q->gidc.p));
+        CUDA_TRY(cudaGetLastError());
+        RankTask& t = tasks[i];
+        t.data = m->data.p;
+        t.rows = m->rows.p;
+        t.indptr = m->indptr.p;
+        t.col_kmin = m->col_kmin.p;
+        t.col_kmax = m->col_kmax.p;
+        t.col_has_zero = m->col_has_zero.p;
+        t.n_rows = R;
+        t.n_cols = (int32_t)C;
+        t.G = (int32_t)q->G;
+        t.group_of_row = q->gidc.p;
+        t.zero_handling = q->opt.zero_handling;
+        t.tie_correction = q->opt.tie_correction;
+        t.group_rows = q->d_group_rows.p;
+        t.U1 = q->U1.p;
+        t.tie = q->P.p;
+        t.n1 = q->n1.p;
+        t.n2 = q->n2.p;
+        t.err = q->err.p;
+    }
+    // one longest-first queue over every (query, gene) item of the batch
+    std::vector<std::pair<long long, int64_t>> it;
+    it.reserve((size_t)items);
+    for (size_t i = 0; i < b.q.size(); ++i) {
+        const hpdex_matrix* m = S->mats[(size_t)b.q[i]->matrix];
+        for (long long c = 0; c < m->n_cols; ++c) it.push_back({m->col_nnz[(size_t)c], ((int64_t)i << 32) | c});
+    }
+    std::stable_sort(it.begin(), it.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    std::vector<int32_t> order(it.size());
+    std::vector<uint16_t> order_task(it.size());
+    for (size_t k = 0; k < it.size(); ++k) {
+        order[k] = (int32_t)(it[k].second & 0xffffffff);
+        order_task[k] = (uint16_t)(it[k].second >> 32);
+    }
+    TRY(b.tasks.alloc(tasks.size()));
+    TRY(b.order.alloc(std::max<size_t>(order.size(), 1)));
+    TRY(b.order_task.alloc(std::max<size_t>(order.size(), 1)));
+    TRY(b.queue.alloc(1));
+    CUDA_TRY(cudaMemcpyAsync(b.tasks.p, tasks.data(), sizeof(RankTask) * tasks.size(), cudaMemcpyHostToDevice, st));
+    if (!order.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(b.order.p, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b.order_task.p, order_task.data(), sizeof(uint16_t) * order.size(), cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(cudaMemsetAsync(b.queue.p, 0, sizeof(int32_t), st));
+
+    // pages of the caller's output arrays that were never written fault one by one when the
+    // device writes them: touch them here
+    for (ServerQuery* q : b.q) {
+        q->direct = S->dev.pageable_access;
+        if (!q->direct) continue;
+        const size_t bytes = sizeof(double) * (size_t)(q->T * S->mats[(size_t)q->matrix]->n_cols);
+        for (size_t o = 0; o < bytes; o += 4096) {
+            reinterpret_cast<volatile unsigned char*>(q->U1_out)[o] = 0;
+            reinterpret_cast<volatile unsigned char*>(q->P_out)[o] = 0;
+        }
+    }
+
+    CUDA_TRY(cudaEventCreate(&b.t0));
+    CUDA_TRY(cudaEventCreate(&b.t1));
+    CUDA_TRY(cudaEventRecord(b.t0, st));
+    if (!order.empty()) {
+        RankArgs a{};
+        a.tasks = b.tasks.p;
+        a.order = b.order.p;
+        a.order_task = b.order_task.p;
+        a.n_order = (int32_t)order.size();
+        a.queue = b.queue.p;
+        a.single_gene = -1;
+        set_layout_args(a, r, GL, b.dk.p, b.dg.p, b.ek.p, b.eg.p, b.acc.p, b.cnt.p);
+        TRY(rank_status(rank_launch(dtype, a, r.grid, r.smem, st), "rank kernel launch"));
+    }
+    for (ServerQuery* q : b.q) {
+        const hpdex_matrix* m = S->mats[(size_t)q->matrix];
+        PArgs pa{};
+        pa.U1 = q->U1.p;
+        pa.P = q->P.p;
+        pa.n = q->T * m->n_cols;
+        pa.n_cols = (int32_t)m->n_cols;
+        pa.col_lo = 0;
+        pa.col_w = (int32_t)m->n_cols;
+        pa.U1_out = q->direct ? q->U1_out : nullptr;
+        pa.P_out = q->direct ? q->P_out : nullptr;
+        pa.group_rows = q->d_group_rows.p;
+        pa.n1g = q->n1.p;
+        pa.n2t = q->n2.p;
+        pa.zero_handling = q->opt.zero_handling;
+        pa.alternative = q->opt.alternative;
+        pa.cc = q->opt.use_continuity ? 0.5 : 0.0;
+        if (pa.n) {
+            const int grid = (int)std::min<long long>((pa.n + 255) / 256, (long long)S->dev.sms * 8);
+            mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, st>>>(pa);
+            CUDA_TRY(cudaGetLastError());
+        }
+    }
+    CUDA_TRY(cudaEventRecord(b.t1, st));
+    return HPDEX_OK;
+}
+
+// Marks a query finished (caller holds S->mu) and releases its workspace.
+void server_finish_query(hpdex_server* S, ServerQuery* q, int status, const std::string& msg) {
+    q->status = status;
+    q->error = msg;
+    q->t_done = std::chrono::steady_clock::now();
+    q->d_gid.alloc(0);
+    q->gidc.alloc(0);
+    q->d_group_rows.alloc(0);
+    q->U1.alloc(0);
+    q->P.alloc(0);
+    q->n1.alloc(0);
+    q->n2.alloc(0);
+    q->err.alloc(0);
+    S->used -= std::min(S->used, q->need);
+    S->completed += 1;
+}
+
+// Results and errors of a finished batch.
+void server_complete(hpdex_server* S, ServerBatch& b) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, b.t0, b.t1);
+    std::vector<std::pair<int, std::string>> res;
+    for (ServerQuery* q : b.q) {
+        unsigned long long e[kErrWords];
+        std::string msg;
+        int st = HPDEX_OK;
+        if (cudaMemcpy(e, q->err.p, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            st = HPDEX_ERR_CUDA;
+            msg = "reading the error words failed";
+        } else {
+            st = decode_errors(e, q->G, &msg);
+        }
+        if (st == HPDEX_OK && !q->direct) {
+            const size_t n = (size_t)(q->T * S->mats[(size_t)q->matrix]->n_cols);
+            if (cudaMemcpy(q->U1_out, q->U1.p, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                cudaMemcpy(q->P_out, q->P.p, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+                st = HPDEX_ERR_CUDA;
+                msg = "copying the results failed";
+            }
+        }
+        res.push_back({st, msg});
+    }
+    std::lock_guard<std::mutex> lock(S->mu);
+    for (size_t i = 0; i < b.q.size(); ++i) server_finish_query(S, b.q[i], res[i].first, res[i].second);
+    S->batches += 1;
+    S->busy_ms += ms;
+    S->cv_done.notify_all();
+}
+
+void server_loop(hpdex_server* S) {
+    cudaSetDevice(S->dev.device);
+    std::deque<std::unique_ptr<ServerBatch>> inflight;
+    for (;;) {
+        // retire finished batches
+        while (!inflight.empty()) {
+            const cudaError_t e = cudaEventQuery(inflight.front()->t1);
+            if (e == cudaErrorNotReady) break;
+            cudaGetLastError();
+            server_complete(S, *inflight.front());
+            inflight.pop_front();
+        }
+        // admit the next batch while fewer than two are queued on the GPU
+        std::unique_ptr<ServerBatch> b;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (inflight.empty() && S->pending.empty()) {
+                if (S->stop) break;
+                S->cv_work.wait(lk, [&] { return S->stop || !S->pending.empty(); });
+                if (S->stop && S->pending.empty()) break;
+            }
+            if (inflight.size() < 2 && !S->pending.empty()) {
+                b.reset(new ServerBatch());
+                int dtype = -1;
+                while (!S->pending.empty() && (int)b->q.size() < S->max_batch) {
+                    ServerQuery* q = S->pending.front();
+                    const int dt = S->mats[(size_t)q->matrix]->dtype;
+                    if (dtype >= 0 && dt != dtype) break;
+                    // a query larger than the whole budget runs alone on an idle server
+                    const bool alone = b->q.empty() && inflight.empty() && S->used == 0;
+                    if (S->used + q->need > S->budget && !alone) break;
+                    S->pending.pop_front();
+                    S->used += q->need;
+                    dtype = dt;
+                    b->q.push_back(q);
+                }
+                if (b->q.empty()) b.reset();
+            }
+            if (!b && !inflight.empty()) {
+                // nothing to admit: wait for the oldest batch, or for a new arrival
+                S->cv_work.wait_for(lk, std::chrono::microseconds(50));
+                continue;
+            }
+        }
+        if (!b) continue;
+        if (server_launch(S, *b) != HPDEX_OK) {
+            const std::string msg = hpdex_last_error();
+            cudaStreamSynchronize(S->stream);
+            std::lock_guard<std::mutex> lock(S->mu);
+            for (ServerQuery* q : b->q) server_finish_query(S, q, HPDEX_ERR_CUDA, msg);
+            S->cv_done.notify_all();
+            continue;
+        }
+        inflight.push_back(std::move(b));
+    }
+    for (auto& x : inflight) {
+        cudaEventSynchronize(x->t1);
+        server_complete(S, *x);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hpdex_server_create(int64_t workspace_bytes, int32_t max_batch, hpdex_server** out) {
+    if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (workspace_bytes <= 0) return fail(HPDEX_ERR_ARGUMENT, "workspace_bytes must be positive");
+    if (max_batch < 1 || max_batch > 65535) return fail(HPDEX_ERR_ARGUMENT, "max_batch must be in 1..65535");
+    std::unique_ptr<hpdex_server> S(new hpdex_server());
+    TRY(device_info(S->dev));
+    S->budget = (size_t)workspace_bytes;
+    S->max_batch = max_batch;
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    hpdex_server* raw = S.get();
+    S->worker = std::thread([raw] { server_loop(raw); });
+    *out = S.release();
+    return HPDEX_OK;
+}
+
+int hpdex_server_add_matrix(hpdex_server* s, hpdex_matrix* m, int32_t* matrix_id) {
+    if (!s || !m || !matrix_id) return fail(HPDEX_ERR_ARGUMENT, "NULL server, matrix or id pointer");
+    if (m->dev.device != s->dev.device) return fail(HPDEX_ERR_ARGUMENT, "matrix and server are on different devices");
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->mats.push_back(m);
+    *matrix_id = (int32_t)(s->mats.size() - 1);
+    return HPDEX_OK;
+}
+
+int hpdex_server_submit(hpdex_server* s, int32_t matrix_id, const int32_t* group_id,
+                        int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out,
+                        double* P_out, int64_t* query_id) {
+    if (!s || !opt || !query_id || !U1_out || !P_out) return fail(HPDEX_ERR_ARGUMENT, "NULL argument");
+    if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    if (n_targets >= (1ll << 30)) return fail(HPDEX_ERR_UNSUPPORTED, "n_targets too large");
+    if (opt->method != HPDEX_ASYMPTOTIC) return fail(HPDEX_ERR_UNSUPPORTED, "the serving loop computes asymptotic p-values only");
+    if (opt->zero_handling < 0 || opt->zero_handling > 3) return fail(HPDEX_ERR_ARGUMENT, "zero_handling must be 0..3");
+    if (opt->alternative < 0 || opt->alternative > 2) return fail(HPDEX_ERR_ARGUMENT, "alternative must be 0..2");
+    hpdex_matrix* m = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (matrix_id < 0 || (size_t)matrix_id >= s->mats.size()) return fail(HPDEX_ERR_ARGUMENT, "unknown matrix id %d", matrix_id);
+        m = s->mats[(size_t)matrix_id];
+    }
+    const long long R = m->n_rows, G = n_targets + 1;
+    if (R > 0 && !group_id) return fail(HPDEX_ERR_ARGUMENT, "group_id is NULL");
+    std::unique_ptr<ServerQuery> q(new ServerQuery());
+    q->matrix = matrix_id;
+    q->T = n_targets;
+    q->G = G;
+    q->opt = *opt;
+    q->gid.assign(group_id, group_id + R);
+    q->group_rows.assign((size_t)G, 0);
+    for (long long r = 0; r < R; ++r) {
+        const int g = group_id[r];
+        if (g >= 0 && g < G) ++q->group_rows[(size_t)g];
+    }
+    if (opt->zero_handling != HPDEX_ZERO_NONE && m->n_cols > 0) {  // as hpdex_plan_create
+        if (q->group_rows[0] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column 0");
+        for (long long g = 1; g < G; ++g)
+            if (q->group_rows[(size_t)g] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for group %lld at column 0", g);
+    }
+    q->U1_out = U1_out;
+    q->P_out = P_out;
+    q->need = query_workspace(m, n_targets, G, opt->zero_handling);
+    q->t_submit = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->stop) return fail(HPDEX_ERR_RUNTIME, "the server is shutting down");
+    q->id = s->next_id++;
+    *query_id = q->id;
+    s->pending.push_back(q.get());
+    s->queries[q->id] = std::move(q);
+    s->cv_work.notify_one();
+    return HPDEX_OK;
+}
+
+int hpdex_server_wait(hpdex_server* s, int64_t query_id, double timeout_s, double* latency_ms) {
+    if (!s) return fail(HPDEX_ERR_ARGUMENT, "server is NULL");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->queries.find(query_id);
+    if (it == s->queries.end()) return fail(HPDEX_ERR_ARGUMENT, "unknown query id %lld", (long long)query_id);
+    ServerQuery* q = it->second.get();
+    auto done = [&] { return q->status >= 0; };
+    if (timeout_s < 0) {
+        s->cv_done.wait(lk, done);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+        return fail(HPDEX_ERR_TIMEOUT, "query %lld still running after %.3f s", (long long)query_id, timeout_s);
+    }
+    if (latency_ms) latency_ms[0] = std::chrono::duration<double, std::milli>(q->t_done - q->t_submit).count();
+    const int st = q->status;
+    const std::string msg = q->error;
+    s->queries.erase(it);
+    if (st != HPDEX_OK) return fail(st, "%s", msg.c_str());
+    return HPDEX_OK;
+}
+
+int hpdex_server_stats(const hpdex_server* s, int64_t* completed, int64_t* batches, double* busy_ms) {
+    if (!s) return fail(HPDEX_ERR_ARGUMENT, "server is NULL");
+    hpdex_server* w = const_cast<hpdex_server*>(s);
+    std::lock_guard<std::mutex> lock(w->mu);
+    if (completed) *completed = s->completed;
+    if (batches) *batches = s->batches;
+    if (busy_ms) *busy_ms = s->busy_ms;
+    return HPDEX_OK;
+}
+
+int hpdex_server_destroy(hpdex_server* s) {
+    if (!s) return HPDEX_OK;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+        while (!s->pending.empty()) {
+            ServerQuery* q = s->pending.front();
+            s->pending.pop_front();
+            q->status = HPDEX_ERR_RUNTIME;
+            q->error = "the server was destroyed before the query ran";
+            q->t_done = std::chrono::steady_clock::now();
+        }
+        s->cv_work.notify_all();
+        s->cv_done.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return HPDEX_OK;
+}
+
+}  // extern "C"
+
+// =======================================================================================
 // No-allocation entry point.
 //
 // For callers that must not allocate device memory during a call: code that runs inside a
@@ -1225,6 +1747,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     unsigned long long* err = reinterpret_cast<unsigned long long*>(take(kErrWords * sizeof(unsigned long long)));
     unsigned long long* max_col = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
     long long* group_rows = reinterpret_cast<long long*>(take(sizeof(long long) * G));
+    RankTask* d_task = reinterpret_cast<RankTask*>(take(sizeof(RankTask)));
     const size_t header_bytes = off;
     int32_t* order = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * std::max<long long>(C, 1)));
     unsigned long long* kmin = reinterpret_cast<unsigned long long*>(take(8 * std::max<long long>(C, 1)));
@@ -1306,29 +1829,34 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
 
     TRY(dispatch_dtype<KeyRangeLaunch>(dtype, d_data, d_indptr, C, kmin, kmax, has_zero, (long long)longest * C,
                                        nd->info.sms, s));
+    RankTask t{};
+    t.data = d_data;
+    t.rows = d_rows;
+    t.indptr = d_indptr;
+    t.col_kmin = kmin;
+    t.col_kmax = kmax;
+    t.col_has_zero = has_zero;
+    t.n_rows = n_rows;
+    t.n_cols = (int32_t)C;
+    t.G = G;
+    t.group_of_row = gidc;
+    t.zero_handling = zh;
+    t.tie_correction = opt->tie_correction;
+    t.group_rows = group_rows;
+    t.U1 = d_U1;
+    t.tie = d_P;
+    t.n1 = n1;
+    t.n2 = n2;
+    t.err = err;
+    CUDA_TRY(cudaMemcpyAsync(d_task, &t, sizeof(RankTask), cudaMemcpyHostToDevice, s));
     RankArgs a{};
-    a.data = d_data;
-    a.rows = d_rows;
-    a.indptr = d_indptr;
-    a.col_kmin = kmin;
-    a.col_kmax = kmax;
-    a.col_has_zero = has_zero;
-    a.n_rows = n_rows;
-    a.n_cols = (int32_t)C;
-    a.n_order = (int32_t)C;
-    a.G = G;
-    a.group_of_row = gidc;
+    a.tasks = d_task;
     a.order = order;
+    a.order_task = nullptr;
+    a.n_order = (int32_t)C;
     a.queue = queue;
     a.single_gene = -1;
-    a.zero_handling = zh;
-    a.tie_correction = opt->tie_correction;
-    a.group_rows = group_rows;
-    a.U1 = d_U1;
-    a.tie = d_P;
-    a.n1 = n1;
-    a.n2 = n2;
-    a.err = err;
+    a.G = G;
     a.dk_global = dk;
     a.dg_global = dg;
     a.ek_global = ek;

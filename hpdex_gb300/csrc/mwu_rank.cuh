@@ -51,7 +51,10 @@ namespace hpdex {
 
 constexpr int kErrWords = 2;  // error words of a run, reset to all ones before it
 
-struct RankArgs {
+// One task = one (resident matrix, grouping) pair with its outputs. A launch ranks the genes
+// of one task, or of several (the serving loop coalesces queries into one launch); the tasks
+// of a launch share the value type and the shared-memory layout (sized for the largest G).
+struct RankTask {
     const void* data;          // values of the CSC matrix (dtype V)
     const int32_t* rows;       // row ids (int32)
     const int64_t* indptr;     // [n_cols + 1]
@@ -60,13 +63,9 @@ struct RankArgs {
     const uint32_t* col_has_zero;        // per column: stores an explicit finite zero
     int64_t n_rows;
     int32_t n_cols;
-    int32_t n_order;           // genes in `order` (all columns, or one chunk of them)
-    int32_t G;                 // n_targets + 1
+    int32_t G;                 // n_targets + 1 (at most the launch's layout G)
     const void* group_of_row;  // [n_rows] group of each row in the kernel's group type
                                // (GroupType below), all ones for rows in no group
-    const int32_t* order;      // genes in processing order [n_order]
-    int32_t* queue;            // work counter (batched form)
-    int32_t single_gene;       // >= 0: plain form, this gene only
     int32_t zero_handling;
     int32_t tie_correction;
     const long long* group_rows;  // [G]
@@ -77,12 +76,22 @@ struct RankArgs {
     unsigned long long* err;   // [0]: min(gene*G + group) of a too-small sample (none)
                                // [1]: min(gene*G + group) of a group with more stored
                                //      entries than rows (duplicate row ids)
+};
+
+struct RankArgs {
+    const RankTask* tasks;     // device array of the launch's tasks
+    const int32_t* order;      // genes in processing order [n_order]
+    const uint16_t* order_task;  // task of each entry of `order` (null: all task 0)
+    int32_t n_order;
+    int32_t* queue;            // work counter (batched form)
+    int32_t single_gene;       // >= 0: plain form, this gene of task 0 only
+    int32_t G;                 // layout G: the largest task G of the launch
     // global scratch, one slice of `slice` elements per CTA for each of:
     void* dk_global;           // decoded keys of the current gene, at the entries' positions
     void* dg_global;           // decoded groups (group type; all ones: not stored)
     void* ek_global;           // bucket-ordered elements of a slab too big for shared memory
     void* eg_global;
-    long long slice;           // rank_slice(longest column): multiple of 64 elements
+    long long slice;           // rank_slice(longest column of any task): multiple of 64
     unsigned char* acc_global; // per CTA 24*G bytes when the accumulators are not in SMEM
     uint32_t* cnt_global;      // per CTA and warp: packed counters (when not in SMEM), then
                                // G 32-bit counters (buckets of more than 65535 elements)
@@ -594,18 +603,18 @@ template <class V, int NT, bool ACC_SMEM>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_gene;
+    __shared__ int s_gene, s_task;
     __shared__ unsigned long long s_tref;
     __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi;
     __shared__ uint32_t s_wsx[32], s_wsy[32];
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int G = a.G, zh = a.zero_handling;
+    const int GL = a.G;  // layout G
     const int NBMAX = 1 << a.nb_max_log2;
-    const RankSmem L(a.nb_max_log2, G, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,
+    const RankSmem L(a.nb_max_log2, GL, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,
                      (int)sizeof(K));
-    const int cw = RankSmem::cnt_words(G);
+    const int cw = RankSmem::cnt_words(GL);
 
     uint32_t* hall = reinterpret_cast<uint32_t*>(smem);  // bucket start (after the scan)
     uint32_t* href = hall + NBMAX + 4;                   // reference elements below a bucket
@@ -613,22 +622,22 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(a.elem_smem_cap);
     unsigned char* accb;
     uint32_t* cnt_base;
-    uint32_t* cnt_glob = a.cnt_global + (size_t)blockIdx.x * a.tie_warps * (cw + G);
+    uint32_t* cnt_glob = a.cnt_global + (size_t)blockIdx.x * a.tie_warps * (cw + GL);
     if constexpr (ACC_SMEM) {
         accb = smem + L.hist_bytes;
         cnt_base = reinterpret_cast<uint32_t*>(smem + L.hist_bytes + L.acc_bytes);
     } else {
-        accb = a.acc_global + (size_t)blockIdx.x * 24 * G;
+        accb = a.acc_global + (size_t)blockIdx.x * 24 * GL;
         cnt_base = cnt_glob;
     }
     unsigned long long* A = reinterpret_cast<unsigned long long*>(accb);
-    unsigned long long* B = A + G;
-    uint32_t* nz = reinterpret_cast<uint32_t*>(B + G);
-    uint32_t* ng = nz + G;
+    unsigned long long* B = A + GL;
+    uint32_t* nz = reinterpret_cast<uint32_t*>(B + GL);
+    uint32_t* ng = nz + GL;
     const Acc acc{A, B};
     uint32_t* wide_base = cnt_glob + (size_t)a.tie_warps * cw;
     uint32_t* cnt = cnt_base + (size_t)warp * cw;
-    uint32_t* wide_cnt = wide_base + (size_t)warp * G;
+    uint32_t* wide_cnt = wide_base + (size_t)warp * GL;
     using GT = GroupType<ACC_SMEM>;
     constexpr uint32_t kNoGroup = ACC_SMEM ? 0xffffu : 0xffffffffu;
     K* ek_s = reinterpret_cast<K*>(smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes);
@@ -638,11 +647,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     K* ek_g = reinterpret_cast<K*>(a.ek_global) + (size_t)blockIdx.x * a.slice;
     GT* eg_g = reinterpret_cast<GT*>(a.eg_global) + (size_t)blockIdx.x * a.slice;
 
-    const GT* gidp = reinterpret_cast<const GT*>(a.group_of_row);
-    const uint32_t nrows = (uint32_t)a.n_rows;
-
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
-    for (int i = tid; i < a.tie_warps * G; i += NT) wide_base[i] = 0u;
+    for (int i = tid; i < a.tie_warps * GL; i += NT) wide_base[i] = 0u;
     if (tid == 0) {
         s_chunk = 0u; s_nbig = 0u; s_bigi = 0u;
     }
@@ -650,34 +656,42 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     bool first = true;
     for (;;) {
         if (tid == 0) {
-            int c = -1;
+            int c = -1, ti = 0;
             if (a.single_gene >= 0) {
                 c = first ? a.single_gene : -1;
             } else {
                 const int gi = atomicAdd(a.queue, 1);
-                c = gi < a.n_order ? a.order[gi] : -1;
+                if (gi < a.n_order) {
+                    c = a.order[gi];
+                    ti = a.order_task ? (int)a.order_task[gi] : 0;
+                }
             }
             s_gene = c;
+            s_task = ti;
             s_tref = 0ull;
             s_maxb = 0u;
         }
         first = false;
-        for (int g = tid; g < G; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
+        for (int g = tid; g < GL; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
         __syncthreads();
         const int c = s_gene;
         if (c < 0) break;
-        const long long p0 = a.indptr[c];
-        const uint32_t nraw = (uint32_t)(a.indptr[c + 1] - p0);
+        const RankTask* tk = a.tasks + s_task;
+        const int G = tk->G, zh = tk->zero_handling;
+        const GT* gidp = reinterpret_cast<const GT*>(tk->group_of_row);
+        const uint32_t nrows = (uint32_t)tk->n_rows;
+        const long long p0 = tk->indptr[c];
+        const uint32_t nraw = (uint32_t)(tk->indptr[c + 1] - p0);
         // entries of this gene, re-based: entry i is rows[i], data[i]; its decoded copy is
         // dk/dg[i]. Passes over the entries go by warp tiles of 128: lane l of a warp takes
         // entries t + l + 32k (k < 4), so that neighbouring lanes read neighbouring entries
         // and their group-id gathers (rows of one column ascend) share L2 sectors.
-        const int32_t* rows = a.rows + p0;
-        const V* data = reinterpret_cast<const V*>(a.data) + p0;
+        const int32_t* rows = tk->rows + p0;
+        const V* data = reinterpret_cast<const V*>(tk->data) + p0;
 
         // ---- bucket function from the column's key range ----
-        K kmin = (K)a.col_kmin[c], kmax = (K)a.col_kmax[c];
-        if (zh == ZH_NONE && a.col_has_zero[c]) {
+        K kmin = (K)tk->col_kmin[c], kmax = (K)tk->col_kmax[c];
+        if (zh == ZH_NONE && tk->col_has_zero[c]) {
             const K kz = Val<V>::key(V(0));
             kmin = kz < kmin ? kz : kmin;
             kmax = kz > kmax ? kz : kmax;
@@ -863,23 +877,23 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         const unsigned long long T_ref = s_tref;
         const unsigned long long nz1 = nz[0];
         for (int g = 1 + tid; g < G; g += NT) {
-            const size_t idx = (size_t)(g - 1) * a.n_cols + c;
+            const size_t idx = (size_t)(g - 1) * tk->n_cols + c;
             const unsigned long long nz2 = nz[g];
             unsigned long long n1, n2, u2x2, ties;
             if (zh == ZH_NONE) {
                 n1 = nz1;
                 n2 = nz2;
-                if (n1 < 2) atomicMin(&a.err[0], (unsigned long long)c * G);
-                else if (n2 < 2) atomicMin(&a.err[0], (unsigned long long)c * G + g);
+                if (n1 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G);
+                else if (n2 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G + g);
                 u2x2 = A[g];
                 ties = T_ref + B[g];
-                a.n2[idx] = (uint32_t)nz2;
-                if (g == 1) a.n1[c] = (uint32_t)nz1;
+                tk->n2[idx] = (uint32_t)nz2;
+                if (g == 1) tk->n1[c] = (uint32_t)nz1;
             } else {
-                n1 = (unsigned long long)a.group_rows[0];
-                n2 = (unsigned long long)a.group_rows[g];
-                if (nz1 > n1) atomicMin(&a.err[1], (unsigned long long)c * G);
-                if (nz2 > n2) atomicMin(&a.err[1], (unsigned long long)c * G + g);
+                n1 = (unsigned long long)tk->group_rows[0];
+                n2 = (unsigned long long)tk->group_rows[g];
+                if (nz1 > n1) atomicMin(&tk->err[1], (unsigned long long)c * G);
+                if (nz2 > n2) atomicMin(&tk->err[1], (unsigned long long)c * G + g);
                 const unsigned long long z1 = n1 - nz1, z2 = n2 - nz2;
                 if (zh == ZH_MIN) u2x2 = A[g] + 2ull * z1 * nz2 + z1 * z2;
                 else if (zh == ZH_MAX) u2x2 = A[g] + z2 * (2ull * nz1 + z1);
@@ -888,8 +902,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 ties = T_ref + B[g] + zz * zz * zz - zz;
             }
             const long long u1x2 = (long long)(2ull * n1 * n2) - (long long)u2x2;
-            a.U1[idx] = (double)u1x2 * 0.5;
-            a.tie[idx] = a.tie_correction ? (double)ties : 0.0;
+            tk->U1[idx] = (double)u1x2 * 0.5;
+            tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
         }
         __syncthreads();
     }

@@ -36,6 +36,7 @@ extern "C" {
 #define HPDEX_ERR_ARGUMENT 2 /* malformed input (sizes, pointers, indptr)              */
 #define HPDEX_ERR_CUDA 3     /* CUDA runtime failure or no usable device               */
 #define HPDEX_ERR_UNSUPPORTED 4
+#define HPDEX_ERR_TIMEOUT 5  /* hpdex_server_wait: the query did not finish in time      */
 
 /* dtype codes of `data` (the reference's TYPE_DISPATCH list, macro.hpp:4-14) */
 #define HPDEX_INT8 0
@@ -182,6 +183,38 @@ int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, const int32_t*
                                const int32_t* d_group_id, int64_t n_targets,
                                const hpdex_mwu_options* opt, double* d_U1, double* d_P,
                                void* stream);
+
+/* ---- serving loop (the reference has none; its DE driver runs one grouping per call) ----
+ *
+ * A server keeps resident matrices (hpdex_matrix handles, borrowed: keep them alive until
+ * the server is destroyed) and answers DE queries -- a grouping and target count over one of
+ * them -- as they arrive. A worker thread admits pending queries in arrival order while their
+ * device workspace (outputs, group ids: about 16 B x n_targets x n_cols + 6 B x n_rows) fits
+ * in `workspace_bytes`, coalesces up to `max_batch` admitted queries of one value dtype into
+ * one launch of the persistent rank kernel (the (query, gene) work items share one
+ * longest-first queue), then runs their p-value kernels and writes U1 and P into the
+ * caller's arrays. The next batch is prepared and queued on the GPU while the previous one
+ * runs. max_batch = 1 gives per-query launches. Asymptotic p-values only.
+ *
+ * hpdex_server_submit copies group_id; U1_out and P_out (n_targets x n_cols doubles,
+ * target-major, host memory) must stay valid until hpdex_server_wait returns for that
+ * query. hpdex_server_wait returns the query's status (HPDEX_OK, or the error the query
+ * raised, with its message for hpdex_last_error), or HPDEX_ERR_TIMEOUT when it is still
+ * running after timeout_s seconds (a negative timeout waits without limit); latency_ms (may
+ * be NULL) is the time from submission to completion. A query is forgotten once waited for.
+ */
+typedef struct hpdex_server hpdex_server;
+int hpdex_server_create(int64_t workspace_bytes, int32_t max_batch, hpdex_server** out);
+int hpdex_server_add_matrix(hpdex_server* s, hpdex_matrix* m, int32_t* matrix_id);
+int hpdex_server_submit(hpdex_server* s, int32_t matrix_id, const int32_t* group_id,
+                        int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out,
+                        double* P_out, int64_t* query_id);
+int hpdex_server_wait(hpdex_server* s, int64_t query_id, double timeout_s, double* latency_ms);
+/* completed queries, launches (batches) and summed GPU busy time (ms) since creation */
+int hpdex_server_stats(const hpdex_server* s, int64_t* completed, int64_t* batches,
+                       double* busy_ms);
+/* finishes the admitted work, fails queries still pending, joins the worker */
+int hpdex_server_destroy(hpdex_server* s);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,54 @@
+"""GPU: the pipelined one-shot call (column chunks uploaded while earlier chunks are ranked,
+p-values written straight into the output arrays on coherent-memory systems) returns what the
+resident path returns, also after the device memory cache is released, and across dtypes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _resident(w, **opt):
+    from hpdex_gb300.resident import ResidentMatrix
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    plan = M.plan(w.group_id, w.n_targets, **opt)
+    plan.run()
+    return plan.download()
+
+
+@pytest.mark.parametrize("zh,zname", [(1, "min"), (2, "max"), (3, "mix")])
+def test_oneshot_equals_resident(zh, zname):
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.perturb_screen(seed=31, n_rows=30_000, n_cols=700, n_targets=40, ref_size=3_000)
+    U1r, Pr = _resident(w, zero_handling=zname, use_continuity=True)
+    for _ in range(2):  # second call reuses cached device memory
+        U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                    use_continuity=True, zero_handling=zh)
+        np.testing.assert_array_equal(U1, U1r)
+        np.testing.assert_array_equal(P, Pr)
+
+
+def test_release_cached_memory_between_calls():
+    import hpdex_gb300
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.umi_counts(seed=6, n_rows=6_000, n_cols=150, n_targets=9)
+    a = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1)
+    hpdex_gb300.release_cached_memory()
+    b = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1)
+    hpdex_gb300.release_cached_memory()
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("dtype", [np.int16, np.uint32, np.float64, np.int64])
+def test_oneshot_dtypes_equal_resident(dtype):
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.umi_counts(seed=12, n_rows=8_000, n_cols=160, n_targets=12)
+    w.data = w.data.astype(dtype)
+    U1r, Pr = _resident(w, zero_handling="min", use_continuity=False)
+    U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                zero_handling=1)
+    np.testing.assert_array_equal(U1, U1r)
+    np.testing.assert_array_equal(P, Pr)
