@@ -43,6 +43,8 @@ EXPORTS = {
     "hpdex_last_error": (ctypes.c_char_p, []),
     "hpdex_device_count": (ctypes.c_int, []),
     "hpdex_release_cached_memory": (ctypes.c_int, []),
+    "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]),
     "hpdex_mannwhitneyu": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,

@@ -94,6 +94,26 @@ int device_info(DeviceInfo& d) {
     return HPDEX_OK;
 }
 
+// The p-value kernels' erfc table (pvalue.cuh), built once per device and process. Called
+// outside stream capture (it synchronises).
+int ensure_erfc_table() {
+    static std::mutex mu;
+    static std::map<int, bool> ready;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (ready[dev]) return HPDEX_OK;
+    cudaStream_t s;
+    CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    erfc_table_kernel<<<(kErfcPoints + 255) / 256, 256, 0, s>>>();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) return fail(HPDEX_ERR_CUDA, "erfc table set-up: %s", cudaGetErrorString(e));
+    ready[dev] = true;
+    return HPDEX_OK;
+}
+
 size_t dtype_size(int dt) {
     switch (dt) {
     case HPDEX_INT8: case HPDEX_UINT8: return 1;
@@ -707,6 +727,24 @@ void hpdex_mwu_options_default(hpdex_mwu_options* o) {
 
 const char* hpdex_last_error(void) { return g_last_error.c_str(); }
 
+int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_err) {
+    if (n_points < 1 || !max_rel_err || !max_abs_err) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    TRY(ensure_erfc_table());
+    DevBuf<unsigned long long> out;
+    TRY(out.alloc(2));
+    CUDA_TRY(cudaMemset(out.p, 0, 2 * sizeof(unsigned long long)));
+    const int grid = (int)std::min<long long>((n_points + 255) / 256, (long long)dev.sms * 8);
+    erfc_check_kernel<<<grid, 256>>>(n_points, out.p, out.p + 1);
+    CUDA_TRY(cudaGetLastError());
+    unsigned long long h[2];
+    CUDA_TRY(cudaMemcpy(h, out.p, sizeof h, cudaMemcpyDeviceToHost));
+    std::memcpy(max_rel_err, &h[0], sizeof(double));
+    std::memcpy(max_abs_err, &h[1], sizeof(double));
+    return HPDEX_OK;
+}
+
 int hpdex_release_cached_memory(void) {
     mem_cache().release_all();
     return HPDEX_OK;
@@ -823,6 +861,7 @@ int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
         TRY(p->n2.alloc(std::max<size_t>(n, 1)));
     }
     TRY(configure_rank(p.get()));
+    TRY(ensure_erfc_table());
     *out = p.release();
     return HPDEX_OK;
 }
@@ -1517,6 +1556,7 @@ int hpdex_server_create(int64_t workspace_bytes, int32_t max_batch, hpdex_server
     if (max_batch < 1 || max_batch > 65535) return fail(HPDEX_ERR_ARGUMENT, "max_batch must be in 1..65535");
     std::unique_ptr<hpdex_server> S(new hpdex_server());
     TRY(device_info(S->dev));
+    TRY(ensure_erfc_table());
     S->budget = (size_t)workspace_bytes;
     S->max_batch = max_batch;
     CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
@@ -1674,6 +1714,7 @@ int noalloc_setup(int dev, NoAllocDevice** out) {
             return fail(HPDEX_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch) failed: %s",
                         cudaGetErrorString(e));
         TRY(device_info(d.info));
+        TRY(ensure_erfc_table());
         d.scratch = static_cast<unsigned char*>(ptr);
     }
     *out = &d;

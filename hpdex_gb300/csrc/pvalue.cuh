@@ -3,7 +3,9 @@
 // Asymptotic: restates the reference's precise path (AI4Cell/hpdex src/cpp/mannwhitneyu.cpp
 // :15-96) with the same double operation order. Every multiply / add / divide / sqrt is an
 // explicitly round-to-nearest intrinsic so that no multiply-add is fused and z is the same
-// double the reference computes; erfc is CUDA's double erfc.
+// double the reference computes. erfc is evaluated from a table (erfc_tab below): FP64 is
+// the scarce pipe on GB300, and the table's Taylor step costs about a tenth of a library
+// erfc, within a few ulp of it.
 //
 // Exact (reference variant): the reference's p_exact (:98-188) is a DP over
 // dp_i[u] = sum_{k=0..n2} dp_{i-1}[u-k] in wrapping uint64 followed by sequential double
@@ -19,6 +21,75 @@
 #include "common.cuh"
 
 namespace hpdex {
+
+// ---------------------------------------------------------------------------------------
+// erfc from a table. erfc is tabulated with its Taylor coefficients at x_k = k / 128,
+// 0 <= x_k < 26.5; for x near x_k, erfc(x_k + d) = sum_n c_n(x_k) d^n with
+//     c_0 = erfc(x_k),   c_n = -(2/sqrt(pi)) exp(-x_k^2) (-1)^(n-1) H_(n-1)(x_k) / n!,
+// from erfc'(x) = -(2/sqrt(pi)) exp(-x^2) and d^m/dx^m exp(-x^2) = (-1)^m H_m(x) exp(-x^2),
+// with the physicists' Hermite polynomials H_0 = 1, H_1 = 2x, H_(m+1) = 2x H_m - 2m H_(m-1).
+// With |d| <= 1/256 the n-th term is about (2 x d)^n / n! of c_0, so 13 terms leave a
+// truncation below 1e-17 relative up to x = 26.5. The sum runs as a Horner polynomial in d;
+// erfc(x_k + d) / erfc(x_k) stays above exp(-0.21), so nothing cancels. The table is built
+// once per device from the CUDA math library's erfc and exp. Beyond 26.5, erfc is below
+// 1e-307 and is returned as 0 (the comparisons of p-values floor at 1e-300); for x < 0,
+// erfc(x) = 2 - erfc(-x).
+// ---------------------------------------------------------------------------------------
+constexpr int kErfcPerUnit = 128;
+constexpr int kErfcTerms = 13;
+constexpr double kErfcXMax = 26.5;
+constexpr int kErfcPoints = (int)(kErfcXMax * kErfcPerUnit) + 2;
+__device__ double g_erfc_table[kErfcPoints * kErfcTerms];
+
+__global__ void erfc_table_kernel() {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kErfcPoints) return;
+    const double x = (double)k / kErfcPerUnit;
+    double* c = g_erfc_table + (size_t)k * kErfcTerms;
+    const double E = 1.1283791670955126 * exp(-x * x);  // 2 / sqrt(pi) * exp(-x^2)
+    c[0] = erfc(x);
+    double hm1 = 0.0, h = 1.0, fact = 1.0, sign = 1.0;  // H_(n-1), n!, (-1)^(n-1)
+    for (int n = 1; n < kErfcTerms; ++n) {
+        fact *= n;
+        c[n] = -E * sign * h / fact;
+        const double hn = 2.0 * x * h - 2.0 * (n - 1) * hm1;  // H_n from H_(n-1), H_(n-2)
+        hm1 = h;
+        h = hn;
+        sign = -sign;
+    }
+}
+
+__device__ __forceinline__ double erfc_tab(double x) {
+    const double ax = fabs(x);
+    double r = 0.0;
+    if (ax < kErfcXMax) {
+        const int k = __double2int_rn(ax * kErfcPerUnit);
+        const double d = ax - (double)k * (1.0 / kErfcPerUnit);  // exact: k / 128
+        const double* c = g_erfc_table + (size_t)k * kErfcTerms;
+        r = c[kErfcTerms - 1];
+#pragma unroll
+        for (int n = kErfcTerms - 2; n >= 0; --n) r = fma(r, d, c[n]);
+    }
+    return x < 0.0 ? 2.0 - r : r;
+}
+
+// Self-check: max relative / absolute difference of erfc_tab against the math library's erfc
+// on n points spread over [-8, 27] (relative only where erfc >= 1e-300).
+__global__ void erfc_check_kernel(long long n, unsigned long long* max_rel_bits,
+                                  unsigned long long* max_abs_bits) {
+    double mr = 0.0, ma = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double x = -8.0 + 35.0 * ((double)i + 0.5) / (double)n;
+        const double a = erfc_tab(x), b = erfc(x);
+        const double e = fabs(a - b);
+        ma = fmax(ma, e);
+        if (b >= 1e-300) mr = fmax(mr, e / b);
+    }
+    // non-negative doubles order like their bit patterns
+    atomicMax(max_rel_bits, (unsigned long long)__double_as_longlong(mr));
+    atomicMax(max_abs_bits, (unsigned long long)__double_as_longlong(ma));
+}
 
 struct PArgs {
     const double* U1;
@@ -72,7 +143,7 @@ __device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, 
         const double U = (U1 > U2 ? U1 : U2);
         if (sigma > 0.0) {
             const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
-            p = __dmul_rn(2.0, __dmul_rn(0.5, erfc(__dmul_rn(z, HPDEX_SQRT1_2))));
+            p = __dmul_rn(2.0, __dmul_rn(0.5, erfc_tab(__dmul_rn(z, HPDEX_SQRT1_2))));
             if (p > 1.0) p = 1.0;
             if (p < 0.0) p = 0.0;
         }
@@ -81,7 +152,7 @@ __device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, 
     const double U = (alt == ALT_LESS) ? __dsub_rn(nm, U1) : U1;
     if (sigma > 0.0) {
         const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
-        p = __dmul_rn(0.5, erfc(__dmul_rn(z, HPDEX_SQRT1_2)));
+        p = __dmul_rn(0.5, erfc_tab(__dmul_rn(z, HPDEX_SQRT1_2)));
     }
     return (p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p));
 }

@@ -93,6 +93,11 @@ int hpdex_device_count(void);
  * reuse by later calls (no cudaMalloc/cudaFree per call); this returns it to the driver. */
 int hpdex_release_cached_memory(void);
 
+/* Self-check of the p-value stage's table-based erfc against the CUDA math library's erfc
+ * on n_points points spread over [-8, 27]: the largest relative difference (where erfc >=
+ * 1e-300) and the largest absolute difference. */
+int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_err);
+
 /* ---- one-shot calls (reference semantics; host pointers in and out) ---- */
 
 /* kernel.mannwhitneyu. threads is accepted for signature parity and only affects host-side

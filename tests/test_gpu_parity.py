@@ -113,3 +113,14 @@ def test_batched_and_plain_forms_agree_and_repeat():
     for U, P in ((U1b, Pb), (U1c, Pc)):
         np.testing.assert_array_equal(U, U1a)
         np.testing.assert_array_equal(P, Pa)
+
+
+def test_erfc_table_against_math_library():
+    """The p-value stage's erfc (Taylor steps from a table, pvalue.cuh) against CUDA's erfc on
+    two million points over [-8, 27]."""
+    import ctypes
+    from hpdex_gb300 import _lib
+    rel, ab = ctypes.c_double(), ctypes.c_double()
+    _lib.check(_lib.lib().hpdex_selftest_erfc(2_000_000, ctypes.byref(rel), ctypes.byref(ab)))
+    assert rel.value <= 2e-15, rel.value
+    assert ab.value <= 1e-15, ab.value
