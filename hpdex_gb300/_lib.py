@@ -45,6 +45,9 @@ EXPORTS = {
     "hpdex_release_cached_memory": (ctypes.c_int, []),
     "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_bh_fdr": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "hpdex_fold_change": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                         ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
     "hpdex_mannwhitneyu": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
@@ -127,3 +130,25 @@ def device_count() -> int:
 def release_cached_memory() -> None:
     """Return the device memory that finished calls keep cached for reuse to the driver."""
     check(lib().hpdex_release_cached_memory())
+
+
+def bh_fdr(p):
+    """Benjamini-Hochberg adjusted p-values on the device (scipy's false_discovery_control)."""
+    import numpy as np
+    p = np.ascontiguousarray(np.asarray(p, dtype=np.float64)).reshape(-1)
+    out = np.empty_like(p)
+    check(lib().hpdex_bh_fdr(p.ctypes.data, p.size, out.ctypes.data))
+    return out
+
+
+def fold_change(means_gene_major, n_genes: int, n_groups: int, clip_value: float):
+    """(fold, log2 fold), each (n_groups - 1, n_genes), from gene-major group means."""
+    import numpy as np
+    m = np.ascontiguousarray(np.asarray(means_gene_major, dtype=np.float64)).reshape(-1)
+    if m.size != n_genes * n_groups:
+        raise ValueError("means must hold n_genes * n_groups values")
+    fold = np.empty((max(n_groups - 1, 0), n_genes), np.float64)
+    log2fold = np.empty_like(fold)
+    check(lib().hpdex_fold_change(m.ctypes.data, int(n_genes), int(n_groups), float(clip_value),
+                                  fold.ctypes.data, log2fold.ctypes.data))
+    return fold, log2fold

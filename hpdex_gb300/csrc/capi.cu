@@ -25,6 +25,7 @@
 
 #include "../../include/hpdex_gb300.h"
 #include "common.cuh"
+#include "fdr.cuh"
 #include "group_mean.cuh"
 #include "mwu_rank.cuh"
 #include "pvalue.cuh"
@@ -745,6 +746,81 @@ int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_e
     return HPDEX_OK;
 }
 
+int hpdex_bh_fdr(const double* p, int64_t n, double* fdr) {
+    if (n < 0 || (n > 0 && (!p || !fdr))) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    if (n <= 1) {
+        if (n == 1) {
+            if (!(p[0] >= 0.0 && p[0] <= 1.0)) return fail(HPDEX_ERR_ARGUMENT, "All values in `ps` must lie between 0. and 1.");
+            fdr[0] = p[0];
+        }
+        return HPDEX_OK;
+    }
+    if (n >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "at most 2^31 - 1 p-values");
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    const int nb = (int)((n + kSortTile - 1) / kSortTile);
+    DevBuf<unsigned long long> k0, k1;
+    DevBuf<uint32_t> v0, v1, counts, bad;
+    DevBuf<double> agg, carry, out;
+    TRY(k0.alloc((size_t)n));
+    TRY(k1.alloc((size_t)n));
+    TRY(v0.alloc((size_t)n));
+    TRY(v1.alloc((size_t)n));
+    TRY(counts.alloc((size_t)256 * nb));
+    TRY(bad.alloc(1));
+    TRY(agg.alloc((size_t)nb));
+    TRY(carry.alloc((size_t)nb));
+    TRY(out.alloc((size_t)n));
+    cudaStream_t s = 0;
+    CUDA_TRY(cudaMemcpyAsync(k0.p, p, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemsetAsync(bad.p, 0, sizeof(uint32_t), s));
+    canonical_zero_kernel<<<std::min(nb, dev.sms * 8), 256, 0, s>>>(k0.p, n);
+    unsigned long long* kin = k0.p;
+    unsigned long long* kout = k1.p;
+    uint32_t* vin = nullptr;
+    uint32_t* vout = v1.p;
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 8 * pass;
+        radix_count_kernel<<<nb, kSortThreads, 0, s>>>(kin, n, shift, counts.p, nb);
+        radix_scan_kernel<<<1, 1024, 0, s>>>(counts.p, (long long)256 * nb);
+        radix_scatter_kernel<<<nb, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, counts.p, nb);
+        CUDA_TRY(cudaGetLastError());
+        std::swap(kin, kout);
+        vin = vout;
+        vout = (vout == v1.p) ? v0.p : v1.p;
+    }
+    bh_block_min_kernel<<<nb, kSortThreads, 0, s>>>(kin, n, agg.p, bad.p);
+    bh_carry_kernel<<<1, 1024, 0, s>>>(agg.p, nb, carry.p);
+    bh_apply_kernel<<<nb, kSortThreads, 0, s>>>(kin, vin, n, carry.p, out.p);
+    CUDA_TRY(cudaGetLastError());
+    uint32_t bad_h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&bad_h, bad.p, sizeof bad_h, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    if (bad_h) return fail(HPDEX_ERR_ARGUMENT, "All values in `ps` must lie between 0. and 1.");
+    CUDA_TRY(cudaMemcpy(fdr, out.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return HPDEX_OK;
+}
+
+int hpdex_fold_change(const double* means, int64_t n_genes, int64_t n_groups, double clip,
+                      double* fold, double* log2fold) {
+    if (n_genes < 0 || n_groups < 1 || !means || !fold || !log2fold) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    const long long n = (n_groups - 1) * n_genes;
+    if (n == 0) return HPDEX_OK;
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    DevBuf<double> dm, df, dl;
+    TRY(dm.alloc((size_t)(n_genes * n_groups)));
+    TRY(df.alloc((size_t)n));
+    TRY(dl.alloc((size_t)n));
+    CUDA_TRY(cudaMemcpy(dm.p, means, sizeof(double) * n_genes * n_groups, cudaMemcpyHostToDevice));
+    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)dev.sms * 8);
+    fold_change_kernel<<<grid, 256>>>(dm.p, n_genes, (int)n_groups, clip, df.p, dl.p);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpy(fold, df.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(log2fold, dl.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return HPDEX_OK;
+}
+
 int hpdex_release_cached_memory(void) {
     mem_cache().release_all();
     return HPDEX_OK;
@@ -1222,6 +1298,11 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
 // =======================================================================================
 namespace {
 
+// A batch stops growing once its queries hold this many matrix entries (about a millisecond
+// of rank work on GB300): coalescing pays for small queries, whose launches would leave SMs
+// idle, while a large query gains nothing from company and its neighbours would wait for it.
+constexpr long long kServerBatchEntries = 48ll << 20;
+
 struct ServerQuery {
     int64_t id = 0;
     int matrix = 0;
@@ -1508,10 +1589,14 @@ void server_loop(hpdex_server* S) {
             if (inflight.size() < 2 && !S->pending.empty()) {
                 b.reset(new ServerBatch());
                 int dtype = -1;
+                long long entries = 0;
                 while (!S->pending.empty() && (int)b->q.size() < S->max_batch) {
                     ServerQuery* q = S->pending.front();
                     const int dt = S->mats[(size_t)q->matrix]->dtype;
                     if (dtype >= 0 && dt != dtype) break;
+                    const long long e = S->mats[(size_t)q->matrix]->nnz;
+                    if (!b->q.empty() && entries + e > kServerBatchEntries) break;
+                    entries += e;
                     // a query larger than the whole budget runs alone on an idle server
                     const bool alone = b->q.empty() && inflight.empty() && S->used == 0;
                     if (S->used + q->need > S->budget && !alone) break;

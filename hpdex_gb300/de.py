@@ -28,9 +28,11 @@ COLUMNS = ["target", "feature", "p_value", "u_statistic", "fold_change", "log2_f
 
 
 def _bh(P: np.ndarray) -> np.ndarray:
-    from scipy.stats import false_discovery_control
+    """BH FDR on the device: scipy.stats.false_discovery_control(P, method="bh"), as the
+    reference driver calls it (de.py:174-184), with its NaN fallback on failure."""
+    from ._lib import bh_fdr
     try:
-        return false_discovery_control(P, method="bh")
+        return bh_fdr(P)
     except Exception:
         logger.warning("FDR correction failed, falling back to NaN")
         return np.full_like(P, np.nan)
@@ -88,14 +90,10 @@ def differential_expression(X, labels, reference, features=None, groups=None,
         group_id[labels == g] = idx
     n_targets = len(groups)
 
-    means = group_mean(matrix, group_id, n_targets + 1, include_zeros=True,
-                       threads=threads).reshape(n_genes, n_targets + 1).T
-    ref_means, tar_means = means[0], means[1:]
-    with np.errstate(divide="ignore", invalid="ignore"):
-        fold = tar_means / ref_means
-        fold = np.where(ref_means < 1e-10, clip_value, fold)
-        fold = np.where(tar_means < 1e-10, 1.0 / clip_value, fold)
-        log2fold = np.log2(fold)
+    # fold change and log2 fold change on the device from the group means (de.py:138-142)
+    from ._lib import fold_change
+    means = group_mean(matrix, group_id, n_targets + 1, include_zeros=True, threads=threads)
+    fold, log2fold = fold_change(means, n_genes, n_targets + 1, clip_value)
 
     U1, P = mannwhitneyu(matrix, group_id, n_targets, ref_sorted=False, tar_sorted=False,
                          use_continuity=use_continuity, tie_correction=tie_correction,

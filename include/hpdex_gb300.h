@@ -93,6 +93,18 @@ int hpdex_device_count(void);
  * reuse by later calls (no cudaMalloc/cudaFree per call); this returns it to the driver. */
 int hpdex_release_cached_memory(void);
 
+/* ---- DE post-processing on the device (the reference DE driver does these on the host,
+ * de.py:138-142 and :174-184) ----
+ * hpdex_bh_fdr: Benjamini-Hochberg adjusted p-values of p[0..n), as
+ * scipy.stats.false_discovery_control(p, method="bh") (values outside [0, 1] or NaN:
+ * HPDEX_ERR_ARGUMENT with scipy's message). hpdex_fold_change: from per-(gene, group) means
+ * (gene-major [gene * n_groups + g], g = 0 the reference) the fold change and log2 fold
+ * change per (target, gene), target-major: tar / ref, `clip` where ref < 1e-10, 1 / clip
+ * where tar < 1e-10. Host pointers in and out. */
+int hpdex_bh_fdr(const double* p, int64_t n, double* fdr);
+int hpdex_fold_change(const double* means, int64_t n_genes, int64_t n_groups, double clip,
+                      double* fold, double* log2fold);
+
 /* Self-check of the p-value stage's table-based erfc against the CUDA math library's erfc
  * on n_points points spread over [-8, 27]: the largest relative difference (where erfc >=
  * 1e-300) and the largest absolute difference. */
