@@ -29,6 +29,7 @@
 #include "group_mean.cuh"
 #include "mwu_rank.cuh"
 #include "pvalue.cuh"
+#include "transpose.cuh"
 #include "rank_launch.h"
 
 using namespace hpdex;
@@ -702,9 +703,77 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
     return HPDEX_OK;
 }
 
+// Device transpose of a cells x genes CSR into the resident CSC layout (transpose.cuh).
+template <class V>
+struct TransposeLaunch {
+    static int run(hpdex_matrix* m, const void* h_data, const int64_t* h_genes, const int64_t* h_rowptr) {
+        const long long R = m->n_rows, C = m->n_cols, nnz_in = m->nnz;
+        const size_t vs = sizeof(V);
+        DevBuf<unsigned char> dval;
+        DevBuf<int64_t> dgen, dptr, col_total;
+        DevBuf<uint32_t> cnt;
+        TRY(dval.alloc(std::max<size_t>(1, (size_t)nnz_in * vs)));
+        TRY(dgen.alloc(std::max<long long>(1, nnz_in)));
+        TRY(dptr.alloc((size_t)R + 1));
+        TRY(col_total.alloc(std::max<long long>(C, 1)));
+        if (nnz_in) {
+            CUDA_TRY(cudaMemcpy(dval.p, h_data, (size_t)nnz_in * vs, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(dgen.p, h_genes, sizeof(int64_t) * nnz_in, cudaMemcpyHostToDevice));
+        }
+        CUDA_TRY(cudaMemcpy(dptr.p, h_rowptr, sizeof(int64_t) * (R + 1), cudaMemcpyHostToDevice));
+        TRY(m->indptr.alloc((size_t)C + 1));
+        const long long nb0 = std::max<long long>(1, std::min<long long>(R, (long long)m->dev.sms * 4));
+        const long long rpb = std::max<long long>(1, (R + nb0 - 1) / nb0);
+        const int nb = (int)std::max<long long>(1, (R + rpb - 1) / rpb);
+        TRY(cnt.alloc((size_t)nb * std::max<long long>(C, 1)));
+        const size_t smem = sizeof(uint32_t) * (size_t)C;
+        const bool in_smem = smem <= 160 * 1024;
+        if (in_smem) {
+            CUDA_TRY(cudaFuncSetAttribute(csr_block_count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(csr_scatter_kernel<V, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            csr_block_count_kernel<true><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
+        } else {
+            CUDA_TRY(cudaMemset(cnt.p, 0, sizeof(uint32_t) * (size_t)nb * C));
+            csr_block_count_kernel<false><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
+        }
+        CUDA_TRY(cudaGetLastError());
+        if (C) {
+            csr_column_scan_kernel<<<(int)((C + 255) / 256), 256>>>(cnt.p, nb, (int)C, col_total.p);
+            column_pointer_scan_kernel<<<1, 1024>>>(col_total.p, (int)C, m->indptr.p);
+            CUDA_TRY(cudaGetLastError());
+        } else {
+            CUDA_TRY(cudaMemset(m->indptr.p, 0, sizeof(int64_t)));
+        }
+        std::vector<int64_t> ip((size_t)C + 1);
+        CUDA_TRY(cudaMemcpy(ip.data(), m->indptr.p, sizeof(int64_t) * (C + 1), cudaMemcpyDeviceToHost));
+        m->nnz = ip[(size_t)C];  // entries with a gene id outside [0, C) are dropped
+        TRY(m->data.alloc(std::max<size_t>(1, (size_t)m->nnz * vs)));
+        TRY(m->rows.alloc(std::max<long long>(1, m->nnz)));
+        if (in_smem)
+            csr_scatter_kernel<V, true><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
+                                                                       (int)C, cnt.p, m->indptr.p, m->rows.p,
+                                                                       reinterpret_cast<V*>(m->data.p));
+        else
+            csr_scatter_kernel<V, false><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
+                                                                  (int)C, cnt.p, m->indptr.p, m->rows.p,
+                                                                  reinterpret_cast<V*>(m->data.p));
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaDeviceSynchronize());
+        m->col_nnz.resize((size_t)C);
+        m->max_col_nnz = 0;
+        for (long long c = 0; c < C; ++c) {
+            m->col_nnz[(size_t)c] = ip[(size_t)c + 1] - ip[(size_t)c];
+            m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
+        }
+        return HPDEX_OK;
+    }
+};
+
 int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
                       int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
                       int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out);
+int matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
+                      int32_t include_zeros, double* out);
 int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
                 const hpdex_mwu_options* opt, hpdex_plan** out, bool lpt_order);
 
@@ -1052,6 +1121,59 @@ int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
     hpdex_matrix* m = nullptr;
     TRY(hpdex_matrix_create(dtype, data, indices, indptr, n_rows, n_cols, nnz, &m));
     std::unique_ptr<hpdex_matrix> hold(m);
+    return matrix_group_mean(m, group_id, n_groups, include_zeros, out);
+}
+
+int hpdex_matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
+                            int32_t include_zeros, double* out) {
+    if (!m) return fail(HPDEX_ERR_ARGUMENT, "matrix is NULL");
+    if (n_groups <= 0 || m->n_cols <= 0) return HPDEX_OK;
+    if (n_groups >= (1ll << 30)) return fail(HPDEX_ERR_UNSUPPORTED, "n_groups too large");
+    return matrix_group_mean(m, group_id, n_groups, include_zeros, out);
+}
+
+int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indices,
+                            const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                            hpdex_matrix** out) {
+    if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (dtype_size(dtype) == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
+    if (!indptr || (nnz > 0 && (!data || !indices))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    if (n_rows < 0 || n_cols < 0 || nnz < 0) return fail(HPDEX_ERR_ARGUMENT, "negative matrix size");
+    if (n_rows >= (1ll << 31) || n_cols >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "n_rows and n_cols must be below 2^31");
+    for (long long r = 0; r < n_rows; ++r)
+        if (indptr[r] < 0 || indptr[r + 1] < indptr[r] || indptr[r + 1] > nnz)
+            return fail(HPDEX_ERR_ARGUMENT, "indptr is not a valid CSR row pointer at row %lld", r);
+    std::unique_ptr<hpdex_matrix> m(new hpdex_matrix());
+    m->dtype = dtype;
+    m->n_rows = n_rows;
+    m->n_cols = n_cols;
+    m->nnz = nnz;
+    TRY(device_info(m->dev));
+    TRY(dispatch_dtype<TransposeLaunch>(dtype, m.get(), data, indices, indptr));
+    TRY(m->col_kmin.alloc(std::max<long long>(n_cols, 1)));
+    TRY(m->col_kmax.alloc(std::max<long long>(n_cols, 1)));
+    TRY(m->col_has_zero.alloc(std::max<long long>(n_cols, 1)));
+    if (n_cols) {
+        TRY(dispatch_dtype<KeyRangeLaunch>(dtype, (const void*)m->data.p, (const int64_t*)m->indptr.p, m->n_cols,
+                                           m->col_kmin.p, m->col_kmax.p, m->col_has_zero.p, m->nnz, m->dev.sms,
+                                           (cudaStream_t)0));
+        CUDA_TRY(cudaDeviceSynchronize());
+    }
+    *out = m.release();
+    return HPDEX_OK;
+}
+
+}  // extern "C"
+
+// =======================================================================================
+// Group means of a resident matrix (reference group_mean_core, mannwhitneyu.cpp:1118-1192).
+// =======================================================================================
+namespace {
+int matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
+                      int32_t include_zeros, double* out) {
+    const long long n_rows = m->n_rows, n_cols = m->n_cols;
+    if (n_rows > 0 && !group_id) return fail(HPDEX_ERR_ARGUMENT, "group_id is NULL");
     std::vector<long long> rows_per((size_t)n_groups, 0);
     for (long long r = 0; r < n_rows; ++r) {
         const int g = group_id[r];
@@ -1089,13 +1211,12 @@ int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
         TRY(acc.alloc((size_t)grid * need));
         a.acc_global = acc.p;
     }
-    TRY(dispatch_dtype<MeanLaunch>(dtype, &a, dim3(grid), smem, (cudaStream_t)0));
+    TRY(dispatch_dtype<MeanLaunch>(m->dtype, &a, dim3(grid), smem, (cudaStream_t)0));
     CUDA_TRY(cudaDeviceSynchronize());
     CUDA_TRY(cudaMemcpy(out, dout.p, sizeof(double) * n_cols * n_groups, cudaMemcpyDeviceToHost));
     return HPDEX_OK;
 }
-
-}  // extern "C"
+}  // namespace
 
 // =======================================================================================
 // Pipelined one-shot call (asymptotic method).

@@ -17,9 +17,7 @@ from __future__ import annotations
 import logging
 
 import numpy as np
-import scipy.sparse
 
-from .backend import group_mean, mannwhitneyu
 
 logger = logging.getLogger(__name__)
 
@@ -36,16 +34,6 @@ def _bh(P: np.ndarray) -> np.ndarray:
     except Exception:
         logger.warning("FDR correction failed, falling back to NaN")
         return np.full_like(P, np.nan)
-
-
-def _to_csc(X):
-    if isinstance(X, np.ndarray):
-        return scipy.sparse.csc_matrix(X)
-    if isinstance(X, scipy.sparse.csr_matrix):
-        return X.tocsc()
-    if isinstance(X, scipy.sparse.csc_matrix):
-        return X
-    return scipy.sparse.csc_matrix(X)
 
 
 def _select_groups(labels, reference, groups, min_samples):
@@ -76,8 +64,7 @@ def differential_expression(X, labels, reference, features=None, groups=None,
         raise ValueError(f"Unsupported metric: {metric}; supported: {supported_metrics}")
     labels = np.asarray(labels, dtype=object)
     groups = _select_groups(labels, reference, groups, min_samples)
-    matrix = _to_csc(X)
-    n_genes = matrix.shape[1]
+    n_genes = X.shape[1]
     features = np.asarray(features if features is not None else np.arange(n_genes), dtype=object)
     if not groups:
         return {c: np.zeros(0, dtype=object if c in ("target", "feature") else np.float64)
@@ -90,14 +77,19 @@ def differential_expression(X, labels, reference, features=None, groups=None,
         group_id[labels == g] = idx
     n_targets = len(groups)
 
-    # fold change and log2 fold change on the device from the group means (de.py:138-142)
+    # one upload serves the means and the tests: CSC as is, a cells x genes CSR transposed on
+    # the device (the reference converts with tocsc() on the host, de.py:106-107)
     from ._lib import fold_change
-    means = group_mean(matrix, group_id, n_targets + 1, include_zeros=True, threads=threads)
+    from .resident import ResidentMatrix
+    M = ResidentMatrix.from_scipy(X)
+    # fold change and log2 fold change on the device from the group means (de.py:138-142)
+    means = M.group_mean(group_id, n_targets + 1, include_zeros=True)
     fold, log2fold = fold_change(means, n_genes, n_targets + 1, clip_value)
 
-    U1, P = mannwhitneyu(matrix, group_id, n_targets, ref_sorted=False, tar_sorted=False,
-                         use_continuity=use_continuity, tie_correction=tie_correction,
-                         zero_handling="min", threads=threads, show_progress=show_progress)
+    plan = M.plan(group_id, n_targets, use_continuity=use_continuity,
+                  tie_correction=tie_correction, zero_handling="min")
+    plan.run()
+    U1, P = plan.download()
     U1 = np.asarray(U1).reshape(-1)
     P = np.asarray(P).reshape(-1)
     return {

@@ -52,8 +52,49 @@ class ResidentMatrix:
         self._h = h
 
     @classmethod
-    def from_scipy(cls, csc):
-        return cls(csc.data, csc.indices, csc.indptr, csc.shape[0])
+    def from_scipy(cls, X):
+        """A cells x genes scipy matrix: CSC as is, CSR transposed on the device."""
+        import scipy.sparse as sp
+        if isinstance(X, sp.csr_matrix):
+            return cls.from_csr(X.data, X.indices, X.indptr, X.shape[0], X.shape[1])
+        X = X if isinstance(X, sp.csc_matrix) else sp.csc_matrix(X)
+        return cls(X.data, X.indices, X.indptr, X.shape[0])
+
+    @classmethod
+    def from_csr(cls, data, indices, indptr, n_rows, n_cols):
+        """A cells x genes CSR (AnnData's native layout), transposed to CSC on the device."""
+        self = cls.__new__(cls)
+        data = np.ascontiguousarray(data)
+        if data.dtype.name not in _lib.DTYPE_CODES:
+            raise RuntimeError("Unsupported dtype for data")
+        indices = np.ascontiguousarray(indices, dtype=np.int64)
+        indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+        self.n_rows, self.n_cols, self.dtype = int(n_rows), int(n_cols), data.dtype
+        if indptr.size != self.n_rows + 1:
+            raise ValueError("indptr must hold n_rows + 1 entries")
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().hpdex_matrix_create_csr(_lib.DTYPE_CODES[data.dtype.name],
+                                                      data.ctypes.data, indices.ctypes.data,
+                                                      indptr.ctypes.data, self.n_rows,
+                                                      self.n_cols, data.size, ctypes.byref(h)))
+        self._h = h
+        self.nnz = self._info()[2]
+        return self
+
+    def _info(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(_lib.lib().hpdex_matrix_info(self._h, *[ctypes.byref(x) for x in v]))
+        return [x.value for x in v]
+
+    def group_mean(self, group_id, n_groups, include_zeros=True):
+        """Per (gene, group) means, flat [gene * n_groups + g] (the reference's layout)."""
+        gid = np.ascontiguousarray(np.asarray(group_id), dtype=np.int32)
+        if gid.size != self.n_rows:
+            raise ValueError(f"group_id has {gid.size} entries, the matrix {self.n_rows} rows")
+        out = np.zeros(max(self.n_cols, 0) * max(int(n_groups), 0), np.float64)
+        _lib.check(_lib.lib().hpdex_matrix_group_mean(self._h, gid.ctypes.data, int(n_groups),
+                                                      int(bool(include_zeros)), out.ctypes.data))
+        return out
 
     def device_bytes(self) -> int:
         v = [ctypes.c_int64() for _ in range(4)]

@@ -138,6 +138,16 @@ typedef struct hpdex_plan hpdex_plan;
 int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
                         const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
                         hpdex_matrix** out);
+/* The same resident matrix from a cells x genes CSR (AnnData's native layout; indptr over
+ * the n_rows cells, indices = gene ids in [0, n_cols)), transposed on the device: columns hold
+ * their rows in ascending order, entries with a gene id outside [0, n_cols) are dropped. */
+int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indices,
+                            const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                            hpdex_matrix** out);
+/* Per (gene, group) means of a resident matrix, flat [gene * n_groups + g]: the values of
+ * hpdex_group_mean (reference group_mean_core, include_zeros as there). */
+int hpdex_matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
+                            int32_t include_zeros, double* out);
 int hpdex_matrix_destroy(hpdex_matrix* m);
 int hpdex_matrix_info(const hpdex_matrix* m, int64_t* n_rows, int64_t* n_cols, int64_t* nnz,
                       int64_t* device_bytes);
