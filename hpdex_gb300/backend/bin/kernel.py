@@ -9,7 +9,10 @@ by the GB300 library through its C ABI (include/hpdex_gb300.h). Differences, by 
   * layout="csr" means the arrays describe a genes x cells CSR matrix (the wrapper's
     contract, mannwhitneyu_.py:51-58), which is the same memory as a cells x genes CSC; the
     reference's binding swaps the row/column counts for CSR instead (module.cpp:51-58).
-  * fast_norm is accepted; p-values always come from the precise erfc path.
+  * fast_norm=True (the binding's default, as in the reference) selects the reference's fast
+    normal tail, its scalar form (Numerical Recipes erfcc, ~1e-7 relative); the reference's
+    vectorised form nests the polynomial differently, so its fast values are not reproduced
+    bit for bit. The wrapper hpdex_gb300.backend.mannwhitneyu defaults to fast_norm=False.
   * threads only affects host-side preparation.
 """
 from __future__ import annotations
@@ -56,7 +59,7 @@ def _options(ref_sorted, tar_sorted, tie_correction, use_continuity, fast_norm, 
     o.tar_sorted = int(bool(tar_sorted))
     o.tie_correction = int(bool(tie_correction))
     o.use_continuity = int(bool(use_continuity))
-    o.fast_norm = 0
+    o.fast_norm = int(bool(fast_norm))
     o.zero_handling = int(zero_handling)
     o.alternative = int(alternative)
     o.method = int(method)

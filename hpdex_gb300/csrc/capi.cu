@@ -533,6 +533,7 @@ int launch_pvalues_asymptotic(hpdex_plan* p, cudaStream_t s) {
     a.zero_handling = p->opt.zero_handling;
     a.alternative = p->opt.alternative;
     a.cc = p->opt.use_continuity ? 0.5 : 0.0;
+    a.fast = p->opt.fast_norm;
     if (a.n == 0) return HPDEX_OK;
     const int grid = (int)std::min<long long>((a.n + 255) / 256, (long long)p->m->dev.sms * 8);
     mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, s>>>(a);
@@ -1385,6 +1386,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         pa.zero_handling = opt->zero_handling;
         pa.alternative = opt->alternative;
         pa.cc = opt->use_continuity ? 0.5 : 0.0;
+        pa.fast = opt->fast_norm;
         if (direct && k == 0) {
             CUDA_TRY(cudaLaunchHostFunc(sc, [](void* f) {
                 const auto* done = static_cast<const std::atomic<int>*>(f);
@@ -1627,6 +1629,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         pa.zero_handling = q->opt.zero_handling;
         pa.alternative = q->opt.alternative;
         pa.cc = q->opt.use_continuity ? 0.5 : 0.0;
+        pa.fast = q->opt.fast_norm;
         if (pa.n) {
             const int grid = (int)std::min<long long>((pa.n + 255) / 256, (long long)S->dev.sms * 8);
             mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, st>>>(pa);
@@ -2131,6 +2134,7 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     pa.zero_handling = zh;
     pa.alternative = opt->alternative;
     pa.cc = opt->use_continuity ? 0.5 : 0.0;
+    pa.fast = opt->fast_norm;
     mwu_pvalue_asymptotic_kernel<<<(int)std::min<long long>((pa.n + 255) / 256, (long long)nd->info.sms * 8), 256, 0, s>>>(pa);
     CUDA_TRY(cudaGetLastError());
 

@@ -105,6 +105,7 @@ struct PArgs {
     int32_t zero_handling;
     int32_t alternative;
     double cc;
+    int32_t fast;              // fast_norm: the reference's fast normal tail (p_asymptotic_fast)
 };
 
 // test i of the column range -> its target t and column c, at idx = t * n_cols + c
@@ -157,6 +158,39 @@ __device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, 
     return (p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p));
 }
 
+// fast_norm = true: the reference's scalar fast path (AI4Cell/hpdex src/cpp/include/
+// common.hpp:14-92), restated: erfc from the Chebyshev fit erfcc of Numerical Recipes (Press et
+// al., section 6.2; fractional error below 1.2e-7) with the math library's exp, mu and
+// 1/sigma as precompute_mu_inv_sd computes them, z = (|U1 - mu| - cc) / sigma two-sided,
+// (U1 - mu - cc) / sigma greater, (U1 - mu + cc) / sigma with p = 1 - sf less. (The
+// reference's vectorised variant of the same polynomial nests its terms differently, so its
+// values depend on the host's vector width; the scalar form is the one restated here.)
+__device__ __forceinline__ double erfcc_nr(double x) {
+    const double ax = fabs(x);
+    const double t = 1.0 / (1.0 + 0.5 * ax);
+    const double tau = t * exp(-ax * ax - 1.26551223 +
+                               t * (1.00002368 + t * (0.37409196 + t * (0.09678418 +
+                               t * (-0.18628806 + t * (0.27886807 + t * (-1.13520398 +
+                               t * (1.48851587 + t * (-0.82215223 + t * 0.17087277)))))))));
+    double r = (x >= 0.0) ? tau : 2.0 - tau;
+    return r < 0.0 ? 0.0 : (r > 2.0 ? 2.0 : r);
+}
+
+__device__ __forceinline__ double p_asymptotic_fast(double U1, double n1, double n2,
+                                                    double tie_sum, double cc, int alt) {
+    const double N = n1 + n2;
+    const double mu = 0.5 * n1 * n2;
+    const double denom = N * (N - 1.0);
+    const double base = n1 * n2 / 12.0;
+    const double var = (denom > 0.0) ? base * (N + 1.0 - tie_sum / denom) : n1 * n2 * (N + 1.0) / 12.0;
+    const double inv_sd = (var <= 0.0) ? 0.0 : 1.0 / sqrt(var);
+    if (inv_sd == 0.0) return 1.0;
+    const double s2 = sqrt(2.0);
+    if (alt == ALT_TWO_SIDED) return 2.0 * (0.5 * erfcc_nr(((fabs(U1 - mu) - cc) * inv_sd) / s2));
+    if (alt == ALT_GREATER) return 0.5 * erfcc_nr(((U1 - mu - cc) * inv_sd) / s2);
+    return 1.0 - 0.5 * erfcc_nr(((U1 - mu + cc) * inv_sd) / s2);
+}
+
 __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
@@ -165,7 +199,8 @@ __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
         double n1, n2;
         test_sizes(a, t, c, idx, n1, n2);
         const double u1 = a.U1[idx];
-        const double p = p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative);
+        const double p = a.fast ? p_asymptotic_fast(u1, n1, n2, a.P[idx], a.cc, a.alternative)
+                                : p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative);
         if (a.P_out) {
             a.U1_out[idx] = u1;
             a.P_out[idx] = p;

@@ -22,8 +22,10 @@ BATCHED, PLAIN = 0, 1
 
 
 def make_options(tie_correction=True, use_continuity=False, zero_handling="mix",
-                 alternative="two-sided", method="asymptotic", exact_variant="reference"):
+                 alternative="two-sided", method="asymptotic", exact_variant="reference",
+                 fast_norm=False):
     o = _lib.MwuOptions()
+    o.fast_norm = int(bool(fast_norm))
     o.tie_correction = int(bool(tie_correction))
     o.use_continuity = int(bool(use_continuity))
     o.zero_handling = _ZH[zero_handling] if isinstance(zero_handling, str) else int(zero_handling)

@@ -218,6 +218,42 @@ double oracle_p_asymptotic(double U1, double n1, double n2, double tie_sum, doub
     return (p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p));
 }
 
+/* fast_norm path (src/cpp/include/common.hpp:14-92, scalar form): Numerical Recipes' erfcc
+ * Chebyshev fit with libm exp; mu and 1/sigma as precompute_mu_inv_sd; two-sided
+ * z = (|U1 - mu| - cc) / sigma, greater (U1 - mu - cc) / sigma, less (U1 - mu + cc) / sigma
+ * with p = 1 - sf. */
+static double erfcc_nr(double x) {
+    const double ax = fabs(x);
+    const double t = 1.0 / (1.0 + 0.5 * ax);
+    const double tau = t * exp(-ax * ax - 1.26551223 +
+                               t * (1.00002368 + t * (0.37409196 + t * (0.09678418 +
+                               t * (-0.18628806 + t * (0.27886807 + t * (-1.13520398 +
+                               t * (1.48851587 + t * (-0.82215223 + t * 0.17087277)))))))));
+    double r = (x >= 0.0) ? tau : 2.0 - tau;
+    return r < 0.0 ? 0.0 : (r > 2.0 ? 2.0 : r);
+}
+
+double oracle_p_asymptotic_fast(double U1, double n1, double n2, double tie_sum, double cc, int alternative) {
+    const double N = n1 + n2;
+    const double mu = 0.5 * n1 * n2;
+    const double denom = N * (N - 1.0);
+    const double base = n1 * n2 / 12.0;
+    const double var = (denom > 0.0) ? base * (N + 1.0 - tie_sum / denom) : n1 * n2 * (N + 1.0) / 12.0;
+    const double inv_sd = (var <= 0.0) ? 0.0 : 1.0 / sqrt(var);
+    if (inv_sd == 0.0) return 1.0;
+    const double s2 = sqrt(2.0);
+    if (alternative == ALT_TWO_SIDED) return 2.0 * (0.5 * erfcc_nr(((fabs(U1 - mu) - cc) * inv_sd) / s2));
+    if (alternative == ALT_GREATER) return 0.5 * erfcc_nr(((U1 - mu - cc) * inv_sd) / s2);
+    return 1.0 - 0.5 * erfcc_nr(((U1 - mu + cc) * inv_sd) / s2);
+}
+
+void oracle_p_asymptotic_fast_array(const double* U1, const double* n1, const double* n2,
+                                    const double* tie_sum, double cc, int alternative, int64_t n,
+                                    double* out) {
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = oracle_p_asymptotic_fast(U1[i], n1[i], n2[i], tie_sum[i], cc, alternative);
+}
+
 /* p_exact (mannwhitneyu.cpp:98-188): the reference's counting DP. Its recurrence
  * dp_i[u] = sum_{k=0..n2} dp_{i-1}[u-k], applied n1 times, counts compositions of u
  * into n1 parts in [0, n2] (not the MWU null), in uint64 arithmetic that wraps. The

@@ -53,6 +53,8 @@ def lib():
         L.oracle_p_asymptotic.restype = d
         L.oracle_p_exact_reference.argtypes = [d, i64, i64]
         L.oracle_p_exact_reference.restype = d
+        L.oracle_p_asymptotic_fast_array.argtypes = [vp, vp, vp, vp, d, i32, i64, vp]
+        L.oracle_p_asymptotic_fast_array.restype = None
         L.oracle_max_threads.argtypes = []
         L.oracle_max_threads.restype = i32
         _LIB = L
@@ -86,6 +88,15 @@ def mannwhitneyu(data, indices, indptr, group_id, n_targets, ref_sorted=False, t
     if st != 0:
         raise RuntimeError(err.value.decode())
     return U1[:n], P[:n]
+
+
+def p_asymptotic_fast(U1, n1, n2, tie_sum, cc, alternative):
+    """The reference's fast_norm p-values (scalar form) from per-test statistics."""
+    arrs = [np.ascontiguousarray(np.asarray(a, dtype=np.float64)).reshape(-1) for a in (U1, n1, n2, tie_sum)]
+    out = np.empty_like(arrs[0])
+    lib().oracle_p_asymptotic_fast_array(*[a.ctypes.data for a in arrs], ctypes.c_double(cc),
+                                         int(alternative), arrs[0].size, out.ctypes.data)
+    return out
 
 
 def mwu_stats(data, indices, indptr, group_id, n_targets, zero_handling):

@@ -23,7 +23,7 @@ def test_oneshot_equals_resident(zh, zname):
     U1r, Pr = _resident(w, zero_handling=zname, use_continuity=True)
     for _ in range(2):  # second call reuses cached device memory
         U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
-                                    use_continuity=True, zero_handling=zh)
+                                    use_continuity=True, zero_handling=zh, fast_norm=False)
         np.testing.assert_array_equal(U1, U1r)
         np.testing.assert_array_equal(P, Pr)
 
@@ -33,9 +33,9 @@ def test_release_cached_memory_between_calls():
     from hpdex_gb300 import synthetic
     from hpdex_gb300.backend.bin import kernel
     w = synthetic.umi_counts(seed=6, n_rows=6_000, n_cols=150, n_targets=9)
-    a = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1)
+    a = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1, fast_norm=False)
     hpdex_gb300.release_cached_memory()
-    b = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1)
+    b = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, zero_handling=1, fast_norm=False)
     hpdex_gb300.release_cached_memory()
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
@@ -49,6 +49,6 @@ def test_oneshot_dtypes_equal_resident(dtype):
     w.data = w.data.astype(dtype)
     U1r, Pr = _resident(w, zero_handling="min", use_continuity=False)
     U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
-                                zero_handling=1)
+                                zero_handling=1, fast_norm=False)
     np.testing.assert_array_equal(U1, U1r)
     np.testing.assert_array_equal(P, Pr)

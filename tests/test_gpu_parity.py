@@ -60,15 +60,16 @@ def _oracle_compare(w, **opt):
     kw = dict(tie_correction=opt.get("tie_correction", True),
               use_continuity=opt.get("use_continuity", True), zero_handling=zh,
               alternative=opt.get("alternative", 2), method=opt.get("method", 2))
+    gkw = dict(kw, fast_norm=False)  # the binding defaults to the fast normal tail
     try:
         U1o, Po = oracle.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
                                       **kw, threads=-1)
     except RuntimeError as e:  # the reference raises: the GPU path must raise the same text
         with pytest.raises(RuntimeError) as e2:
-            kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw)
+            kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **gkw)
         assert str(e2.value) == str(e)
         return "error"
-    U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **kw)
+    U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets, **gkw)
     C, T = w.n_cols, w.n_targets
     np.testing.assert_array_equal(U1, gene_major_to_target_major(U1o, C, T))
     assert_p_close(P, gene_major_to_target_major(Po, C, T))
@@ -124,3 +125,24 @@ def test_erfc_table_against_math_library():
     _lib.check(_lib.lib().hpdex_selftest_erfc(2_000_000, ctypes.byref(rel), ctypes.byref(ab)))
     assert rel.value <= 2e-15, rel.value
     assert ab.value <= 1e-15, ab.value
+
+
+@pytest.mark.parametrize("alt", [0, 1, 2])
+def test_fast_norm_matches_restated_reference_fast_path(alt):
+    """fast_norm=True: the reference's scalar fast normal tail (Numerical Recipes erfcc), here
+    and in the oracle from the same per-test statistics; both are within ~1e-7 of precise."""
+    from oracle import oracle
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.perturb_screen(seed=23, n_rows=12_000, n_cols=200, n_targets=20, ref_size=1_500)
+    U1, P = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                use_continuity=True, zero_handling=1, alternative=alt, fast_norm=True)
+    U1o, n1, n2, tie = oracle.mwu_stats(w.data, w.indices, w.indptr, w.group_id, w.n_targets, 1)
+    C, T = w.n_cols, w.n_targets
+    Pf = oracle.p_asymptotic_fast(U1o, n1, n2, tie, 0.5, alt)
+    np.testing.assert_array_equal(U1, gene_major_to_target_major(U1o, C, T))
+    np.testing.assert_allclose(P, gene_major_to_target_major(Pf, C, T), rtol=1e-12, atol=1e-300)
+    _, Pp = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                use_continuity=True, zero_handling=1, alternative=alt, fast_norm=False)
+    big = Pp > 1e-6
+    assert np.all(np.abs(P[big] - Pp[big]) <= 2e-6 * np.maximum(Pp[big], 1e-3) + 1e-7)

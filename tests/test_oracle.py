@@ -71,3 +71,24 @@ def test_oracle_exact_reference_discrepancy(oracle_lib):
     assert abs(sf - 0.32224) < 1e-15
     from oracle.exact_null import mwu_sf_exact
     assert abs(2 * mwu_sf_exact(12, 5, 4) - 0.7301587301587301) < 1e-15
+
+
+def test_oracle_fast_norm_path_restates_reference_scalar_form():
+    """fast_norm: Numerical Recipes erfcc (fractional error < 1.2e-7 of erfc), the reference's
+    own arithmetic for mu and 1/sigma, and no clip of the two-sided p (|U1 - mu| < cc gives a
+    p above 1, as in the reference's scalar path)."""
+    import math
+    from oracle import oracle
+    rng = np.random.default_rng(0)
+    n1 = rng.integers(5, 400, 500).astype(np.float64)
+    n2 = rng.integers(5, 400, 500).astype(np.float64)
+    U1 = np.floor(rng.random(500) * n1 * n2)
+    tie = np.zeros(500)
+    for alt in (0, 1, 2):
+        pf = oracle.p_asymptotic_fast(U1, n1, n2, tie, 0.5, alt)
+        pp = np.array([oracle.lib().oracle_p_asymptotic(u, a, b, 0.0, 0.5, alt)
+                       for u, a, b in zip(U1, n1, n2)])
+        ok = pp > 1e-12
+        assert np.all(np.abs(pf[ok] - pp[ok]) <= 3e-7 * np.maximum(pp[ok], 1e-2))
+    p = oracle.p_asymptotic_fast([50.0], [10.0], [10.0], [0.0], 0.5, 2)[0]
+    assert p > 1.0 and math.isclose(p, 1.0301501, rel_tol=1e-6)

@@ -22,7 +22,8 @@ def _regular(w, opt):
     return kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
                                tie_correction=bool(opt.tie_correction),
                                use_continuity=bool(opt.use_continuity),
-                               zero_handling=opt.zero_handling, alternative=opt.alternative)
+                               zero_handling=opt.zero_handling, alternative=opt.alternative,
+                               fast_norm=bool(opt.fast_norm))
 
 
 def _noalloc(w, opt, torch):
