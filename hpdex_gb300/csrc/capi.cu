@@ -1233,10 +1233,7 @@ int matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_
 // =======================================================================================
 namespace {
 
-// relative chunk sizes; the compute left after the last copy is about the longest gene of
-// the last chunk, so the last chunk is not made smaller than that needs
-constexpr int kPipelineWeights[] = {4, 4, 4, 4, 4, 4, 4, 3};
-constexpr int kPipelineChunks = sizeof(kPipelineWeights) / sizeof(int);
+constexpr int kPipelineChunks = 12;
 
 int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
                       int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
@@ -1266,24 +1263,25 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         m->col_nnz[(size_t)c] = indptr[c + 1] - indptr[c];
         m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
     }
-    hpdex_plan* praw = nullptr;
-    TRY(plan_create(m.get(), group_id, n_targets, opt, &praw, false));
-    std::unique_ptr<hpdex_plan> p(praw);
-    const long long T = p->T;
-    if (C == 0) return HPDEX_OK;
+    if (C == 0) {
+        hpdex_plan* praw = nullptr;
+        TRY(plan_create(m.get(), group_id, n_targets, opt, &praw, false));
+        delete praw;
+        return HPDEX_OK;
+    }
 
-    // chunks of about nnz / kPipelineChunks entries (whole columns)
+    // equal chunks of about nnz / kPipelineChunks entries (whole columns), uploaded in
+    // descending order of their longest column: the compute left after the last copy is
+    // about the last chunk's longest gene
     std::vector<long long> cb{0};
-    int wsum = 0, wacc = 0;
-    for (int w : kPipelineWeights) wsum += w;
     for (int k = 1; k < kPipelineChunks; ++k) {
-        wacc += kPipelineWeights[k - 1];
-        const long long target = (long long)((double)nnz * wacc / wsum);
+        const long long target = nnz / kPipelineChunks * k;
         const long long c = std::lower_bound(indptr, indptr + C + 1, target) - indptr;
         if (c > cb.back() && c < C) cb.push_back(c);
     }
     cb.push_back(C);
     const int K = (int)cb.size() - 1;
+    std::vector<long long> longest((size_t)K, 0);
     long long max_chunk = 0;
     std::vector<int32_t> order((size_t)C);
     for (int k = 0; k < K; ++k) {
@@ -1291,15 +1289,63 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         auto b = order.begin() + cb[k], e = order.begin() + cb[k + 1];
         std::iota(b, e, (int32_t)cb[k]);
         std::stable_sort(b, e, [&](int32_t x, int32_t y) { return m->col_nnz[(size_t)x] > m->col_nnz[(size_t)y]; });
+        longest[(size_t)k] = m->col_nnz[(size_t)*b];
     }
-    CUDA_TRY(cudaMemcpy(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice));
+    std::vector<int> seq((size_t)K);
+    std::iota(seq.begin(), seq.end(), 0);
+    std::stable_sort(seq.begin(), seq.end(), [&](int x, int y) { return longest[(size_t)x] > longest[(size_t)y]; });
     DevBuf<int32_t> queues;
     DevBuf<long long> stage[2];
     TRY(queues.alloc((size_t)K));
     for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
 
+    struct Res {  // copy stream and events of this call, released once the copy stream drained
+        cudaStream_t copy = nullptr;
+        std::vector<cudaEvent_t> ev;
+        ~Res() {
+            if (copy) cudaStreamSynchronize(copy);
+            for (auto e : ev) if (e) cudaEventDestroy(e);
+            if (copy) cudaStreamDestroy(copy);
+        }
+    } r;
+    CUDA_TRY(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+    r.ev.assign((size_t)(2 * K), nullptr);
+    for (auto& e : r.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaStream_t sx = r.copy;
+    auto enqueue_copy = [&](int j) -> int {  // upload position j: chunk seq[j], staging buffer j & 1
+        const int k = seq[(size_t)j];
+        const long long p0 = indptr[cb[k]], nk = indptr[cb[k + 1]] - p0;
+        if (j >= 2) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (j - 2) + 1], 0));  // staging buffer free
+        if (nk) {
+            CUDA_TRY(cudaMemcpyAsync(m->data.p + p0 * vs, static_cast<const unsigned char*>(data) + p0 * vs,
+                                     (size_t)nk * vs, cudaMemcpyHostToDevice, sx));
+            CUDA_TRY(cudaMemcpyAsync(stage[j & 1].p, indices + p0, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, sx));
+        }
+        CUDA_TRY(cudaEventRecord(r.ev[2 * j], sx));
+        return HPDEX_OK;
+    };
+
+    // the host-side plan (group sizes, reference checks, layout, allocations) runs on a helper
+    // thread while the first chunk is uploaded
+    hpdex_plan* praw = nullptr;
+    int plan_status = HPDEX_OK;
+    std::string plan_error;
+    const int dev_id = m->dev.device;
+    std::thread planner([&] {
+        cudaSetDevice(dev_id);
+        plan_status = plan_create(m.get(), group_id, n_targets, opt, &praw, false);
+        if (plan_status != HPDEX_OK) plan_error = hpdex_last_error();
+    });
+    const int first_copy = enqueue_copy(0);
+    planner.join();
+    std::unique_ptr<hpdex_plan> p(praw);
+    if (plan_status != HPDEX_OK) return fail(plan_status, "%s", plan_error.c_str());
+    TRY(first_copy);
+    const long long T = p->T;
+    CUDA_TRY(cudaMemcpyAsync(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, p->stream));
+
     // Output pages never written before (fresh numpy arrays) would fault one by one when the
-    // device writes them; a host thread touches them while the first chunk is in flight, and
+    // device writes them; a host thread touches them while the first chunks are in flight, and
     // the compute stream waits for it before the first p-value kernel.
     const bool direct = m->dev.pageable_access && U1_out && P_out;
     std::atomic<int> touched{0};
@@ -1317,22 +1363,12 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
             touched.store(1, std::memory_order_release);
         });
     }
-    struct Res {  // streams and events of this call, released after both streams drained
-        cudaStream_t copy = nullptr;
-        std::vector<cudaEvent_t> ev;
-        cudaStream_t comp = nullptr;
-        ~Res() {
-            if (copy) cudaStreamSynchronize(copy);
-            if (comp) cudaStreamSynchronize(comp);
-            for (auto e : ev) if (e) cudaEventDestroy(e);
-            if (copy) cudaStreamDestroy(copy);
-        }
-    } r;
-    r.comp = p->stream;
-    CUDA_TRY(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
-    r.ev.assign((size_t)(2 * K), nullptr);
-    for (auto& e : r.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    cudaStream_t sc = r.comp, sx = r.copy;
+    cudaStream_t sc = p->stream;
+    // every exit drains the compute stream before the plan, the toucher flag or the buffers go
+    struct Drain {
+        cudaStream_t s;
+        ~Drain() { cudaStreamSynchronize(s); }
+    } drain{sc};
 
     CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), sc));
     CUDA_TRY(cudaMemsetAsync(queues.p, 0, sizeof(int32_t) * K, sc));
@@ -1344,24 +1380,17 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
             prepare_group_ids_kernel<uint32_t><<<grid, 256, 0, sc>>>(p->gid.p, n_rows, (int32_t)p->G, reinterpret_cast<uint32_t*>(p->gidc.p));
         CUDA_TRY(cudaGetLastError());
     }
-    for (int k = 0; k < K; ++k) {
+    for (int j = 0; j < K; ++j) {
+        const int k = seq[(size_t)j];
         const long long c0 = cb[k], c1 = cb[k + 1];
         const long long p0 = indptr[c0], nk = indptr[c1] - p0;
-        cudaEvent_t copied = r.ev[2 * k], narrowed = r.ev[2 * k + 1];
-        if (k >= 2) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (k - 2) + 1], 0));  // staging buffer free
-        if (nk) {
-            CUDA_TRY(cudaMemcpyAsync(m->data.p + p0 * vs, static_cast<const unsigned char*>(data) + p0 * vs,
-                                     (size_t)nk * vs, cudaMemcpyHostToDevice, sx));
-            CUDA_TRY(cudaMemcpyAsync(stage[k & 1].p, indices + p0, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, sx));
-        }
-        CUDA_TRY(cudaEventRecord(copied, sx));
-        CUDA_TRY(cudaStreamWaitEvent(sc, copied, 0));
+        CUDA_TRY(cudaStreamWaitEvent(sc, r.ev[2 * j], 0));
         if (nk) {
             narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sc>>>(
-                stage[k & 1].p, m->rows.p + p0, nk, n_rows);
+                stage[j & 1].p, m->rows.p + p0, nk, n_rows);
             CUDA_TRY(cudaGetLastError());
         }
-        CUDA_TRY(cudaEventRecord(narrowed, sc));
+        CUDA_TRY(cudaEventRecord(r.ev[2 * j + 1], sc));
         TRY(dispatch_dtype<KeyRangeLaunch>(dtype, (const void*)m->data.p, (const int64_t*)(m->indptr.p + c0), c1 - c0,
                                            m->col_kmin.p + c0, m->col_kmax.p + c0, m->col_has_zero.p + c0, nk,
                                            m->dev.sms, sc));
@@ -1387,7 +1416,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         pa.alternative = opt->alternative;
         pa.cc = opt->use_continuity ? 0.5 : 0.0;
         pa.fast = opt->fast_norm;
-        if (direct && k == 0) {
+        if (direct && j == 0) {
             CUDA_TRY(cudaLaunchHostFunc(sc, [](void* f) {
                 const auto* done = static_cast<const std::atomic<int>*>(f);
                 while (!done->load(std::memory_order_acquire)) std::this_thread::yield();
@@ -1398,6 +1427,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
             mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, sc>>>(pa);
             CUDA_TRY(cudaGetLastError());
         }
+        if (j + 1 < K) TRY(enqueue_copy(j + 1));
     }
     CUDA_TRY(cudaStreamSynchronize(sc));
     TRY(check_device_errors(p.get()));
