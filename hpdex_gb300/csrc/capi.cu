@@ -457,6 +457,10 @@ int rank_layout(const DeviceInfo& dev, int dtype, int G, long long max_col, Rank
     r.cap = (int)std::min<size_t>(left / (r.kb + r.gb + 1), (size_t)1 << 30);  // + big-list entry share
     r.cap = std::max(0, r.cap - 8) & ~7;
     L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.acc_in, r.cap, r.kb);
+    while (L.total > budget && r.cap > 0) {  // the big list is sized for compact slabs
+        r.cap = std::max(0, r.cap - 64);
+        L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.acc_in, r.cap, r.kb);
+    }
     r.smem = L.total;
     int blocks = 0;
     TRY(rank_status(rank_occupancy(dtype, r.smem, dev.smem_optin, r.acc_in, &blocks), "rank kernel set-up"));
@@ -2077,6 +2081,10 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     int cap = (int)std::min<size_t>((budget - L.total) / (kb + gb + 1), (size_t)1 << 30);
     cap = std::max(0, cap - 8) & ~7;
     L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
+    while (L.total > budget && cap > 0) {
+        cap = std::max(0, cap - 64);
+        L = RankSmem(nbl, G, tie_warps, 1, 1, cap, kb);
+    }
     int blocks = 0;
     TRY(rank_status(rank_occupancy(dtype, L.total, nd->info.smem_optin, 1, &blocks), "rank kernel set-up"));
     if (blocks < 1) return fail(HPDEX_ERR_CUDA, "rank kernel does not fit on an SM");

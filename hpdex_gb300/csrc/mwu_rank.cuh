@@ -125,13 +125,18 @@ struct RankSmem {
     size_t hist_bytes, acc_bytes, cnt_bytes, elem_bytes, total;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
     __host__ __device__ static int cnt_words(int G) { return (G + 1) / 2; }
-    // a slab holds at most elem_cap elements outside one oversized bucket, so it has at most
-    // elem_cap / (kMediumBucket + 1) + 2 buckets above kMediumBucket
-    __host__ __device__ static int big_list(int elem_cap) { return elem_cap / 33 + 64; }
+    // elements the element region holds with 16-bit key offsets (compact slabs)
+    __host__ __device__ static int compact_cap(int elem_cap, int key_bytes, int acc_in_smem) {
+        const int gb = group_bytes(acc_in_smem);
+        return (int)(((long long)elem_cap * (key_bytes + gb) / (2 + gb)) & ~7ll);
+    }
+    // a slab holds at most (compact) capacity elements outside one oversized bucket, so it has
+    // at most capacity / (kMediumBucket + 1) + 2 buckets above kMediumBucket
+    __host__ __device__ static int big_list(int max_elems) { return max_elems / 33 + 64; }
     __host__ __device__ RankSmem(int nb_max_log2, int G, int tie_warps, int acc_in_smem,
                                  int cnt_in_smem, int elem_cap, int key_bytes) {
         const size_t NB = size_t(1) << nb_max_log2;
-        hist_bytes = align16((2 * (NB + 4) + big_list(elem_cap)) * 4);
+        hist_bytes = align16((2 * (NB + 4) + big_list(compact_cap(elem_cap, key_bytes, acc_in_smem))) * 4);
         acc_bytes = acc_in_smem ? align16(size_t(G) * 24) : 0;
         cnt_bytes = cnt_in_smem ? align16(size_t(tie_warps) * cnt_words(G) * 4) : 0;
         elem_bytes = align16(size_t(elem_cap) * (key_bytes + group_bytes(acc_in_smem)));
@@ -330,7 +335,8 @@ __device__ __forceinline__ void add_pair(const Acc& acc, uint32_t g, unsigned lo
 //   target: A += 2*(rb + lt) + c0, B += 3c0^2 + 3c0*s + s^2 - 1
 //   reference: T_ref += c0^2 - 1
 // where lt / c0 count the reference elements of the bucket with a smaller / equal key and s
-// the target elements with the same key and group. Summed over a run of c0 reference and
+// the target elements with the same key and group (keys of different buckets are never
+// compared: they may be 16-bit offsets inside their buckets). Summed over a run of c0 reference and
 // s target-g elements these give s*(2*lref + c0), (c0+s)^3-(c0+s)-(c0^3-c0) and c0^3-c0.
 // lt and c0 come from broadcasting the (few) reference lanes; s from the warp's group
 // counters, which show which groups occur more than once in the round, and a pairwise
@@ -370,7 +376,7 @@ __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, un
             const int j = __ffs((int)r) - 1;
             const K kj = __shfl_sync(0xffffffffu, key, j);
             const uint32_t gj = __shfl_sync(0xffffffffu, g, j);
-            c += (gj == g && kj == key);
+            c += ((sub >> j) & 1u) && gj == g && kj == key;  // same bucket: keys may be offsets
         }
         if (ng > 1u) s = c;
     }
@@ -619,7 +625,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     uint32_t* hall = reinterpret_cast<uint32_t*>(smem);  // bucket start (after the scan)
     uint32_t* href = hall + NBMAX + 4;                   // reference elements below a bucket
     uint32_t* biglist = href + NBMAX + 4;                // large buckets of the current slab
-    const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(a.elem_smem_cap);
+    const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(
+        RankSmem::compact_cap(a.elem_smem_cap, (int)sizeof(K), ACC_SMEM));
     unsigned char* accb;
     uint32_t* cnt_base;
     uint32_t* cnt_glob = a.cnt_global + (size_t)blockIdx.x * a.tie_warps * (cw + GL);
@@ -640,8 +647,16 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     uint32_t* wide_cnt = wide_base + (size_t)warp * GL;
     using GT = GroupType<ACC_SMEM>;
     constexpr uint32_t kNoGroup = ACC_SMEM ? 0xffffu : 0xffffffffu;
-    K* ek_s = reinterpret_cast<K*>(smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes);
-    GT* eg_s = reinterpret_cast<GT*>(ek_s + a.elem_smem_cap);
+    // the element region holds a slab either with full keys (cap_full elements) or, when a
+    // bucket spans at most 2^16 keys, with 16-bit offsets of the key inside its bucket
+    // (cap_compact elements): within a bucket the offsets order like the keys
+    unsigned char* elem_base = smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes;
+    const uint32_t cap_full = (uint32_t)a.elem_smem_cap;
+    const uint32_t cap_compact = (uint32_t)RankSmem::compact_cap(a.elem_smem_cap, (int)sizeof(K), ACC_SMEM);
+    K* ek_s = reinterpret_cast<K*>(elem_base);
+    GT* eg_s = reinterpret_cast<GT*>(ek_s + cap_full);
+    uint16_t* eo_s = reinterpret_cast<uint16_t*>(elem_base);
+    GT* ego_s = reinterpret_cast<GT*>(eo_s + cap_compact);
     K* dk = reinterpret_cast<K*>(a.dk_global) + (size_t)blockIdx.x * a.slice;
     GT* dg = reinterpret_cast<GT*>(a.dg_global) + (size_t)blockIdx.x * a.slice;
     K* ek_g = reinterpret_cast<K*>(a.ek_global) + (size_t)blockIdx.x * a.slice;
@@ -765,7 +780,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         __syncthreads();
         block_scan2<NT>(hall, href, NB, s_wsx, s_wsy, &s_maxb);
         const uint32_t n = hall[NB];
-        const uint32_t cap = (uint32_t)a.elem_smem_cap;
+        const bool compact = shift <= 16;
+        const uint32_t cap = compact ? cap_compact : cap_full;
+        const K offmask = compact ? (K)((1u << shift) - 1u) : K(0);
         // slabs: the whole gene when it fits in shared memory; else buckets whose start lies
         // in [k*W, (k+1)*W) form slab k, which holds at most W + (largest bucket) elements:
         // that fits the capacity unless one bucket is larger than half of it (such a slab is
@@ -839,8 +856,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
                             if (!in[k]) continue;
-                            if (in_smem) { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = (GT)g4[k]; }
-                            else { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = (GT)g4[k]; }
+                            if (!in_smem) { ek_g[pos[k]] = k4[k]; eg_g[pos[k]] = (GT)g4[k]; }
+                            else if (compact) { eo_s[pos[k]] = (uint16_t)((k4[k] - kmin) & offmask); ego_s[pos[k]] = (GT)g4[k]; }
+                            else { ek_s[pos[k]] = k4[k]; eg_s[pos[k]] = (GT)g4[k]; }
                         }
                         if (!more) break;
                         t = tn;
@@ -857,7 +875,11 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             }
 
             // ---- rank ----
-            if (in_smem)
+            if (in_smem && compact)
+                rank_slab<uint32_t, ACC_SMEM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
+                                              biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                              wide_cnt, s_tbl[warp], tref);
+            else if (in_smem)
                 rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref);
