@@ -106,6 +106,8 @@ struct RankArgs {
 constexpr int kMediumBucket = 32;  // 2..32: packed whole into warp rounds
 constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum per bucket
 constexpr uint32_t kInvalid = 0xffffffffu;
+constexpr uint32_t kTaken = 0xfffffffeu;    // a big-list entry that a warp has resolved
+constexpr int kDrainWaitIters = 4096;       // polls (with a short sleep) for a big-list entry
 // Group ids inside the kernel: 16-bit when the accumulators are in shared memory (which
 // bounds G far below 65535), else 32-bit; all ones marks an entry outside every group.
 template <bool ACC_SMEM>
@@ -511,10 +513,16 @@ template <class K, bool SH, class EK, class EG>
 __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi, uint32_t base,
                           const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
-                          uint32_t* s_bigi, const Acc& acc, uint32_t* cnt, uint32_t* wide_cnt,
-                          uint8_t* tbl, unsigned long long& tref) {
+                          uint32_t* s_bigi, uint32_t* s_wdone, const Acc& acc, uint32_t* cnt,
+                          uint32_t* wide_cnt, uint8_t* tbl, unsigned long long& tref) {
     const int lane = threadIdx.x & 31;
     const uint32_t nchunks = (bhi - blo + 31u) / 32u;
+    auto resolve_listed = [&](uint32_t b) {
+        const uint32_t sb = (b == blo) ? base : hall[b - 1];
+        const uint32_t m = hall[b] - sb;
+        if (m <= 65535u) resolve_big<K, false, SH, SH>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
+        else resolve_big<K, true, SH, false>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
+    };
     for (;;) {
         uint32_t ch = 0;
         if (lane == 0) ch = atomicAdd(s_chunk, 1u);
@@ -590,19 +598,51 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             else resolve_big<K, true, SH, false>(sj, mj, rj, ek, eg, acc, wide_cnt, tref);
         }
     }
+    // Big buckets: a warp whose chunks are done takes listed buckets while other warps may
+    // still be listing (no barrier between the phases). An entry is published by its slot
+    // (s_nbig) and then its bucket id; a taker waits a bounded time for the id and marks the
+    // entry taken. When every warp has finished its chunks and the taker's index is past the
+    // final count, the list is exhausted. A wait that runs out leaves its entry for the
+    // pass after the barrier, which resolves every entry not marked taken.
+    __threadfence_block();
+    __syncwarp();
+    if (lane == 0) atomicAdd(s_wdone, 1u);
+    const uint32_t nwarps = blockDim.x >> 5;
+    for (;;) {
+        uint32_t b = kInvalid, st = 0;  // st: 0 a bucket, 1 list exhausted, 2 wait ran out
+        if (lane == 0) {
+            const uint32_t q = atomicAdd(s_bigi, 1u);
+            for (int it = 0;; ++it) {
+                const uint32_t nb = min(*(volatile uint32_t*)s_nbig, biglist_cap);
+                if (q < nb) {
+                    const uint32_t v = ((volatile uint32_t*)biglist)[q];
+                    if (v != kInvalid) {
+                        b = v;
+                        biglist[q] = kTaken;
+                        break;
+                    }
+                } else if (*(volatile uint32_t*)s_wdone == nwarps) {
+                    __threadfence_block();
+                    if (q >= min(*(volatile uint32_t*)s_nbig, biglist_cap)) { st = 1; break; }
+                    continue;
+                }
+                if (it >= kDrainWaitIters) { st = 2; break; }
+                __nanosleep(64);
+            }
+        }
+        st = __shfl_sync(0xffffffffu, st, 0);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (st != 0u) break;
+        resolve_listed(b);
+    }
     __syncthreads();
     const uint32_t nbig = min(*s_nbig, biglist_cap);
-    for (;;) {
-        uint32_t q = 0;
-        if (lane == 0) q = atomicAdd(s_bigi, 1u);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= nbig) break;
-        const uint32_t b = biglist[q];
-        const uint32_t sb = (b == blo) ? base : hall[b - 1];
-        const uint32_t m = hall[b] - sb;
-        if (m <= 65535u) resolve_big<K, false, SH, SH>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
-        else resolve_big<K, true, SH, false>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
+    for (uint32_t q = threadIdx.x >> 5; q < nbig; q += nwarps) {
+        const uint32_t v = biglist[q];
+        if (v != kTaken && v != kInvalid) resolve_listed(v);
     }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nbig; q += blockDim.x) biglist[q] = kInvalid;
 }
 
 template <class V, int NT, bool ACC_SMEM>
@@ -611,7 +651,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_gene, s_task;
     __shared__ unsigned long long s_tref;
-    __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi;
+    __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi, s_wdone;
     __shared__ uint32_t s_wsx[32], s_wsy[32];
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
@@ -664,8 +704,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
     for (int i = tid; i < a.tie_warps * GL; i += NT) wide_base[i] = 0u;
+    for (uint32_t i = tid; i < biglist_cap; i += NT) biglist[i] = kInvalid;
     if (tid == 0) {
-        s_chunk = 0u; s_nbig = 0u; s_bigi = 0u;
+        s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; s_wdone = 0u;
     }
 
     bool first = true;
@@ -877,18 +918,18 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             // ---- rank ----
             if (in_smem && compact)
                 rank_slab<uint32_t, ACC_SMEM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
-                                              biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                              biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                               wide_cnt, s_tbl[warp], tref);
             else if (in_smem)
                 rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
-                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref);
             else
                 rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
-                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, acc, cnt,
+                                       biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref);
             __syncthreads();
-            if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; }
+            if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; s_wdone = 0u; }
             blo = bhi;
         }
         tref = warp_sum_u64(tref);
