@@ -45,6 +45,8 @@ EXPORTS = {
     "hpdex_release_cached_memory": (ctypes.c_int, []),
     "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_selftest_division": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64,
+                                               ctypes.POINTER(ctypes.c_int64)]),
     "hpdex_bh_fdr": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "hpdex_fold_change": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
@@ -74,6 +76,7 @@ EXPORTS = {
     "hpdex_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hpdex_plan_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "hpdex_plan_set_fused_pvalues": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                           ctypes.POINTER(ctypes.c_int32)]),
     "hpdex_mannwhitneyu_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,

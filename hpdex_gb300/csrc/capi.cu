@@ -96,15 +96,21 @@ int device_info(DeviceInfo& d) {
     return HPDEX_OK;
 }
 
-// The p-value kernels' erfc table (pvalue.cuh), built once per device and process. Called
+// The p-value stage's erfc table (pvalue.cuh), built once per device and process; *tbl (if
+// given) receives its device address, which the rank kernel's fused p-values read. Called
 // outside stream capture (it synchronises).
-int ensure_erfc_table() {
+int ensure_erfc_table(const double** tbl = nullptr) {
     static std::mutex mu;
-    static std::map<int, bool> ready;
+    static std::map<int, const double*> ready;
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lock(mu);
-    if (ready[dev]) return HPDEX_OK;
+    if (ready[dev]) {
+        if (tbl) *tbl = ready[dev];
+        return HPDEX_OK;
+    }
+    void* addr = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&addr, g_erfc_table));
     cudaStream_t s;
     CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     erfc_table_kernel<<<(kErfcPoints + 255) / 256, 256, 0, s>>>();
@@ -112,7 +118,8 @@ int ensure_erfc_table() {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     if (e != cudaSuccess) return fail(HPDEX_ERR_CUDA, "erfc table set-up: %s", cudaGetErrorString(e));
-    ready[dev] = true;
+    ready[dev] = static_cast<const double*>(addr);
+    if (tbl) *tbl = ready[dev];
     return HPDEX_OK;
 }
 
@@ -262,6 +269,7 @@ struct hpdex_plan {
     std::vector<long long> group_rows;
     DevBuf<int32_t> gid;
     DevBuf<long long> d_group_rows;
+    DevBuf<PConst> d_pconst;  // per-target p-value constants (zero_handling min / max / mix)
     DevBuf<int32_t> order;
     DevBuf<int32_t> queue;
     DevBuf<unsigned long long> err;
@@ -276,6 +284,7 @@ struct hpdex_plan {
     DevBuf<unsigned char> acc;
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
+    bool fused_pvalues = false;  // asymptotic p-values computed inside the rank kernel
     size_t rank_smem = 0;
     int rank_grid = 0;
     // exact tables
@@ -425,7 +434,21 @@ RankTask task_of(const hpdex_matrix* m, const hpdex_plan* p) {
     t.n1 = p->n1.p;
     t.n2 = p->n2.p;
     t.err = p->err.p;
+    t.alternative = p->opt.alternative;
+    t.fast_norm = p->opt.fast_norm;
+    t.cc = p->opt.use_continuity ? 0.5 : 0.0;
+    t.pconst = p->d_pconst.p;
     return t;
+}
+
+// Per-target p-value constants of a grouping (n1 = reference rows, n2 = the target's rows);
+// empty under zero_handling none, where n1 and n2 depend on the gene.
+std::vector<PConst> target_consts(const std::vector<long long>& group_rows, int zero_handling) {
+    std::vector<PConst> k;
+    if (zero_handling == HPDEX_ZERO_NONE) return k;
+    for (size_t g = 1; g < group_rows.size(); ++g)
+        k.push_back(make_pconst((double)group_rows[0], (double)group_rows[g]));
+    return k;
 }
 
 // Rank-kernel layout for this plan: one 1024-thread CTA per SM; the bucket table takes
@@ -534,6 +557,7 @@ int launch_pvalues_asymptotic(hpdex_plan* p, cudaStream_t s) {
     a.group_rows = p->d_group_rows.p;
     a.n1g = p->n1.p;
     a.n2t = p->n2.p;
+    a.pk = p->d_pconst.p;
     a.zero_handling = p->opt.zero_handling;
     a.alternative = p->opt.alternative;
     a.cc = p->opt.use_continuity ? 0.5 : 0.0;
@@ -820,6 +844,24 @@ int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_e
     return HPDEX_OK;
 }
 
+int hpdex_selftest_division(int64_t n_cases, uint64_t seed, int64_t* mismatches) {
+    if (n_cases < 0 || !mismatches) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    DevBuf<unsigned long long> out;
+    TRY(out.alloc(1));
+    CUDA_TRY(cudaMemset(out.p, 0, sizeof(unsigned long long)));
+    if (n_cases) {
+        const int grid = (int)std::min<long long>((n_cases + 255) / 256, (long long)dev.sms * 16);
+        division_check_kernel<<<grid, 256>>>(n_cases, seed, out.p);
+        CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long h = 0;
+    CUDA_TRY(cudaMemcpy(&h, out.p, sizeof h, cudaMemcpyDeviceToHost));
+    *mismatches = (int64_t)h;
+    return HPDEX_OK;
+}
+
 int hpdex_bh_fdr(const double* p, int64_t n, double* fdr) {
     if (n < 0 || (n > 0 && (!p || !fdr))) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
     if (n <= 1) {
@@ -991,6 +1033,13 @@ int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
     if (R) CUDA_TRY(cudaMemcpy(p->gid.p, group_id, sizeof(int32_t) * R, cudaMemcpyHostToDevice));
     TRY(p->d_group_rows.alloc((size_t)G));
     CUDA_TRY(cudaMemcpy(p->d_group_rows.p, p->group_rows.data(), sizeof(long long) * G, cudaMemcpyHostToDevice));
+    {
+        const std::vector<PConst> k = target_consts(p->group_rows, opt->zero_handling);
+        if (!k.empty()) {
+            TRY(p->d_pconst.alloc(k.size()));
+            CUDA_TRY(cudaMemcpy(p->d_pconst.p, k.data(), sizeof(PConst) * k.size(), cudaMemcpyHostToDevice));
+        }
+    }
     // longest genes first: the work queue hands them out before the short tail
     TRY(p->order.alloc(std::max<long long>(C, 1)));
     if (lpt_order && C) {
@@ -1011,7 +1060,12 @@ int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
         TRY(p->n2.alloc(std::max<size_t>(n, 1)));
     }
     TRY(configure_rank(p.get()));
-    TRY(ensure_erfc_table());
+    const double* tbl = nullptr;
+    TRY(ensure_erfc_table(&tbl));
+    if (opt->method == HPDEX_ASYMPTOTIC) {  // p-values inside the rank kernel by default
+        p->fused_pvalues = true;
+        p->ra.erfc_table = tbl;
+    }
     *out = p.release();
     return HPDEX_OK;
 }
@@ -1044,7 +1098,7 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
                 st = fail(HPDEX_ERR_CUDA, "memset failed");
             if (st == HPDEX_OK) st = enqueue_rank(p, mode, s, &l);
             if (st == HPDEX_OK && cudaEventRecordWithFlags(p->ev[1], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
-            if (st == HPDEX_OK) st = launch_pvalues_asymptotic(p, s);
+            if (st == HPDEX_OK && !p->fused_pvalues) st = launch_pvalues_asymptotic(p, s);
             if (st == HPDEX_OK && cudaEventRecordWithFlags(p->ev[2], s, ext) != cudaSuccess) st = fail(HPDEX_ERR_CUDA, "event record failed");
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -1054,7 +1108,7 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
             CUDA_TRY(cudaGraphInstantiate(&p->graph_exec, g, 0));
         }
         CUDA_TRY(cudaGraphLaunch(p->graph_exec, s));
-        launches = (p->m->n_cols > 0 ? 1 : 0) + (p->T * p->m->n_cols > 0 ? 1 : 0);
+        launches = (p->m->n_cols > 0 ? 2 : 0) + (!p->fused_pvalues && p->T * p->m->n_cols > 0 ? 1 : 0);
     } else {
         CUDA_TRY(cudaEventRecord(p->ev[0], s));
         CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), s));
@@ -1063,7 +1117,7 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
         if (exact) {
             TRY(run_exact(p, s));
             launches += 2;
-        } else {
+        } else if (!p->fused_pvalues) {
             TRY(launch_pvalues_asymptotic(p, s));
             launches += 1;
         }
@@ -1075,6 +1129,23 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
     CUDA_TRY(cudaEventElapsedTime(&p->last_ms[1], p->ev[0], p->ev[1]));
     CUDA_TRY(cudaEventElapsedTime(&p->last_ms[2], p->ev[1], p->ev[2]));
     return check_device_errors(p);
+}
+
+int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (p->opt.method != HPDEX_ASYMPTOTIC) {
+        if (on) return fail(HPDEX_ERR_UNSUPPORTED, "fused p-values need method=asymptotic");
+        return HPDEX_OK;
+    }
+    const double* tbl = nullptr;
+    TRY(ensure_erfc_table(&tbl));
+    const bool f = on != 0;
+    if (f == p->fused_pvalues) return HPDEX_OK;
+    p->fused_pvalues = f;
+    p->ra.erfc_table = f ? tbl : nullptr;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return HPDEX_OK;
 }
 
 int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out) {
@@ -1344,6 +1415,10 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     planner.join();
     std::unique_ptr<hpdex_plan> p(praw);
     if (plan_status != HPDEX_OK) return fail(plan_status, "%s", plan_error.c_str());
+    // the p-value kernel of each chunk writes U1 and P (straight into the caller's arrays
+    // where the device can reach them), so the rank kernel keeps the tie sums
+    p->fused_pvalues = false;
+    p->ra.erfc_table = nullptr;
     TRY(first_copy);
     const long long T = p->T;
     CUDA_TRY(cudaMemcpyAsync(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, p->stream));
@@ -1414,6 +1489,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         pa.U1_out = direct ? U1_out : nullptr;
         pa.P_out = direct ? P_out : nullptr;
         pa.group_rows = p->d_group_rows.p;
+        pa.pk = p->d_pconst.p;
         pa.n1g = p->n1.p;
         pa.n2t = p->n2.p;
         pa.zero_handling = opt->zero_handling;
@@ -1473,6 +1549,8 @@ struct ServerQuery {
     DevBuf<int32_t> d_gid;
     DevBuf<unsigned char> gidc;
     DevBuf<long long> d_group_rows;
+    std::vector<PConst> pconst;  // per-target p-value constants (zero_handling min / max / mix)
+    DevBuf<PConst> d_pconst;
     DevBuf<double> U1, P;
     DevBuf<uint32_t> n1, n2;
     DevBuf<unsigned long long> err;
@@ -1568,6 +1646,11 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         TRY(q->err.alloc(kErrWords));
         if (R) CUDA_TRY(cudaMemcpyAsync(q->d_gid.p, q->gid.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemcpyAsync(q->d_group_rows.p, q->group_rows.data(), sizeof(long long) * q->G, cudaMemcpyHostToDevice, st));
+        q->pconst = target_consts(q->group_rows, q->opt.zero_handling);
+        if (!q->pconst.empty()) {
+            TRY(q->d_pconst.alloc(q->pconst.size()));
+            CUDA_TRY(cudaMemcpyAsync(q->d_pconst.p, q->pconst.data(), sizeof(PConst) * q->pconst.size(), cudaMemcpyHostToDevice, st));
+        }
         CUDA_TRY(cudaMemsetAsync(q->err.p, 0xff, kErrWords * sizeof(unsigned long long), st));
         const int grid = (int)std::max<long long>(1, std::min<long long>((R + 255) / 256, (long long)S->dev.sms * 8));
         if (r.acc_in)
@@ -1589,6 +1672,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         t.zero_handling = q->opt.zero_handling;
         t.tie_correction = q->opt.tie_correction;
         t.group_rows = q->d_group_rows.p;
+        t.pconst = q->d_pconst.p;
         t.U1 = q->U1.p;
         t.tie = q->P.p;
         t.n1 = q->n1.p;
@@ -1658,6 +1742,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         pa.U1_out = q->direct ? q->U1_out : nullptr;
         pa.P_out = q->direct ? q->P_out : nullptr;
         pa.group_rows = q->d_group_rows.p;
+        pa.pk = q->d_pconst.p;
         pa.n1g = q->n1.p;
         pa.n2t = q->n2.p;
         pa.zero_handling = q->opt.zero_handling;
@@ -1682,6 +1767,7 @@ void server_finish_query(hpdex_server* S, ServerQuery* q, int status, const std:
     q->d_gid.alloc(0);
     q->gidc.alloc(0);
     q->d_group_rows.alloc(0);
+    q->d_pconst.alloc(0);
     q->U1.alloc(0);
     q->P.alloc(0);
     q->n1.alloc(0);

@@ -5,7 +5,8 @@
 // form. For the gene it computes, for every target g, the exact integers
 //     2*U2[g] = sum over target elements x of (2 * #ref{< x} + #ref{== x})  (+ zero block)
 //     tie[g]  = sum over distinct values of (t^3 - t) in ref u target g
-// and writes U1 = n1*n2 - U2 and the (masked) tie sum; the p-value kernel finishes. This
+// and writes U1 = n1*n2 - U2 and the (masked) tie sum; a p-value kernel finishes, or the
+// kernel computes the p-values itself during the next gene (fused p-values, below). This
 // reproduces the reference's per-(gene, target) merge (AI4Cell/hpdex
 // src/cpp/mannwhitneyu.cpp:618-840, driver :843-1065) without re-walking the reference
 // slice for every target: reference ranks come from one bucket index per gene.
@@ -30,7 +31,7 @@
 //           warps drain one bucket at a time with per-warp group counters: one
 //           representative per (run of equal keys, target) adds s*(2*lref + c0) to A and
 //           (c0+s)^3-(c0+s)-(c0^3-c0) to B
-//   final   zero block, U1, tie sum per target
+//   final   zero block, U1, tie sum per target (fused: P during the next gene's rank phase)
 //
 // Shared-memory accumulators use 32-bit atomics (a 64-bit value is updated as two halves
 // with an explicit carry): on sm_103a a 64-bit shared atomic add costs about five times a
@@ -46,6 +47,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "pvalue_math.cuh"
 
 namespace hpdex {
 
@@ -76,6 +78,11 @@ struct RankTask {
     unsigned long long* err;   // [0]: min(gene*G + group) of a too-small sample (none)
                                // [1]: min(gene*G + group) of a group with more stored
                                //      entries than rows (duplicate row ids)
+    // p-value options, used when the launch computes p-values (RankArgs::erfc_table)
+    int32_t alternative;
+    int32_t fast_norm;
+    double cc;                 // continuity correction (0.5 or 0)
+    const PConst* pconst;      // zero_handling min / max / mix: per target (or null)
 };
 
 struct RankArgs {
@@ -101,6 +108,8 @@ struct RankArgs {
     int32_t acc_in_smem;       // accumulators and packed run counters in shared memory
     int32_t cnt_in_smem;       // (equal to acc_in_smem; kept for the layout arithmetic)
     int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
+    const double* erfc_table;  // non-null: the kernel also computes the asymptotic p-values
+                               // (P replaces the tie sums); null: a p-value kernel follows
 };
 
 constexpr int kMediumBucket = 32;  // 2..32: packed whole into warp rounds
@@ -108,6 +117,8 @@ constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum pe
 constexpr uint32_t kInvalid = 0xffffffffu;
 constexpr uint32_t kTaken = 0xfffffffeu;    // a big-list entry that a warp has resolved
 constexpr int kDrainWaitIters = 4096;       // polls (with a short sleep) for a big-list entry
+constexpr int kPvWarps = 8;                 // warps (two per SM sub-partition) that take a
+                                            // gene's p-value tiles in the next gene's rank phase
 // Group ids inside the kernel: 16-bit when the accumulators are in shared memory (which
 // bounds G far below 65535), else 32-bit; all ones marks an entry outside every group.
 template <bool ACC_SMEM>
@@ -505,6 +516,51 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Fused p-values. A gene's finalize writes U1 and the tie sum of its tests; the FP64 work of
+// turning them into p-values is left pending and done during the next gene's rank phase by
+// kPvWarps warps, while the other warps keep the integer pipes busy (FP64 is the scarce pipe
+// on GB300, and the rank phase hardly uses it). The CTA's last gene is finished by all warps
+// after the work queue runs dry.
+// ---------------------------------------------------------------------------------------
+// Tests of targets 1 + 32q + lane of gene c: P replaces the tie sum. Not inlined, so that the
+// FP64 arithmetic's registers stay out of the rank loops' allocation (one test per lane: more
+// independent chains per warp cost the rank loops more than they gain).
+static __device__ __noinline__ void pvalue_tile(const RankTask* tk, int c, uint32_t q, const double* tbl) {
+    const int g = 1 + 32 * (int)q + (int)(threadIdx.x & 31);
+    if (g >= tk->G) return;
+    const size_t idx = (size_t)(g - 1) * tk->n_cols + c;
+    double n1, n2;
+    if (tk->zero_handling == ZH_NONE) {
+        n1 = (double)tk->n1[c];
+        n2 = (double)tk->n2[idx];
+    } else {
+        n1 = (double)tk->group_rows[0];
+        n2 = (double)tk->group_rows[g];
+    }
+    const double u1 = tk->U1[idx], ts = tk->tie[idx];
+    double p;
+    if (tk->fast_norm) p = p_asymptotic_fast(u1, n1, n2, ts, tk->cc, tk->alternative);
+    else if (tk->pconst && tk->zero_handling != ZH_NONE)
+        p = p_asymptotic_k(u1, tk->pconst[g - 1], ts, tk->cc, tk->alternative, tbl);
+    else p = p_asymptotic(u1, n1, n2, ts, tk->cc, tk->alternative, tbl);
+    tk->tie[idx] = p;
+}
+
+// The calling warp takes tiles of 32 tests of gene c until none is left (*s_pvq counts the
+// tiles taken).
+__device__ __forceinline__ void pvalue_tiles(const RankTask* tk, int c, uint32_t* s_pvq,
+                                             const double* tbl) {
+    const uint32_t ntiles = ((uint32_t)tk->G + 30u) / 32u;  // ceil((G - 1) / 32)
+    for (;;) {
+        uint32_t q = 0;
+        if ((threadIdx.x & 31) == 0) q = atomicAdd(s_pvq, 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= ntiles) break;
+        pvalue_tile(tk, c, q, tbl);
+    }
+}
+
 // Rank phase of one slab: elements [0, cnt) in bucket order in ek/eg, buckets [blo, bhi)
 // starting at `base` in the gene's bucket order (hall[b - 1] = start of bucket b).
 // Buckets of 2..32 elements are packed whole, in bucket order, into rounds of up to 32
@@ -514,9 +570,12 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
                           const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
                           uint32_t* s_bigi, uint32_t* s_wdone, const Acc& acc, uint32_t* cnt,
-                          uint32_t* wide_cnt, uint8_t* tbl, unsigned long long& tref) {
+                          uint32_t* wide_cnt, uint8_t* tbl, unsigned long long& tref,
+                          const RankTask* pv_tk, int pv_c, uint32_t* s_pvq, const double* erfc_table) {
     const int lane = threadIdx.x & 31;
     const uint32_t nchunks = (bhi - blo + 31u) / 32u;
+    // the previous gene's p-values (first slab only): kPvWarps warps, then they join the chunks
+    if (pv_tk && (threadIdx.x >> 5) < (unsigned)kPvWarps) pvalue_tiles(pv_tk, pv_c, s_pvq, erfc_table);
     auto resolve_listed = [&](uint32_t b) {
         const uint32_t sb = (b == blo) ? base : hall[b - 1];
         const uint32_t m = hall[b] - sb;
@@ -652,6 +711,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     __shared__ int s_gene, s_task;
     __shared__ unsigned long long s_tref;
     __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi, s_wdone;
+    __shared__ int s_pv_gene, s_pv_task;  // gene whose p-values are pending (-1: none)
+    __shared__ uint32_t s_pvq;            // its p-value tiles taken so far
     __shared__ uint32_t s_wsx[32], s_wsy[32];
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
@@ -707,6 +768,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     for (uint32_t i = tid; i < biglist_cap; i += NT) biglist[i] = kInvalid;
     if (tid == 0) {
         s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; s_wdone = 0u;
+        s_pv_gene = -1; s_pv_task = 0; s_pvq = 0u;
     }
 
     bool first = true;
@@ -731,7 +793,12 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         for (int g = tid; g < GL; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
         __syncthreads();
         const int c = s_gene;
-        if (c < 0) break;
+        const int pv_c = s_pv_gene;
+        const RankTask* pv_tk = (a.erfc_table && pv_c >= 0) ? a.tasks + s_pv_task : nullptr;
+        if (c < 0) {
+            if (pv_tk) pvalue_tiles(pv_tk, pv_c, &s_pvq, a.erfc_table);
+            break;
+        }
         const RankTask* tk = a.tasks + s_task;
         const int G = tk->G, zh = tk->zero_handling;
         const GT* gidp = reinterpret_cast<const GT*>(tk->group_of_row);
@@ -919,19 +986,24 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             if (in_smem && compact)
                 rank_slab<uint32_t, ACC_SMEM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
                                               biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
-                                              wide_cnt, s_tbl[warp], tref);
+                                              wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
+                                              &s_pvq, a.erfc_table);
             else if (in_smem)
                 rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
-                                       wide_cnt, s_tbl[warp], tref);
+                                       wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
+                                       &s_pvq, a.erfc_table);
             else
                 rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
-                                       wide_cnt, s_tbl[warp], tref);
+                                       wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
+                                       &s_pvq, a.erfc_table);
             __syncthreads();
             if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; s_wdone = 0u; }
             blo = bhi;
         }
+        // pending p-values not taken in the rank phase (a gene without stored elements has none)
+        if (pv_tk) pvalue_tiles(pv_tk, pv_c, &s_pvq, a.erfc_table);
         tref = warp_sum_u64(tref);
         if (lane == 0 && tref) atomicAdd(&s_tref, tref);
         __syncthreads();
@@ -967,6 +1039,11 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             const long long u1x2 = (long long)(2ull * n1 * n2) - (long long)u2x2;
             tk->U1[idx] = (double)u1x2 * 0.5;
             tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
+        }
+        if (tid == 0 && a.erfc_table) {  // this gene's p-values: pending until the next gene
+            s_pv_gene = c;
+            s_pv_task = s_task;
+            s_pvq = 0u;
         }
         __syncthreads();
     }

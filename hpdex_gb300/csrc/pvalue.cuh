@@ -1,11 +1,9 @@
 // pvalue.cuh -- p-value stage of the MWU backend (sm_103a).
 //
-// Asymptotic: restates the reference's precise path (AI4Cell/hpdex src/cpp/mannwhitneyu.cpp
-// :15-96) with the same double operation order. Every multiply / add / divide / sqrt is an
-// explicitly round-to-nearest intrinsic so that no multiply-add is fused and z is the same
-// double the reference computes. erfc is evaluated from a table (erfc_tab below): FP64 is
-// the scarce pipe on GB300, and the table's Taylor step costs about a tenth of a library
-// erfc, within a few ulp of it.
+// Asymptotic: mwu_pvalue_asymptotic_kernel applies the per-test arithmetic of
+// pvalue_math.cuh (the reference's precise path, AI4Cell/hpdex src/cpp/mannwhitneyu.cpp:15-96,
+// in the same double operation order, erfc from a table) to a column range of the rank
+// kernel's outputs. The rank kernel can also run the same arithmetic itself (fused p-values).
 //
 // Exact (reference variant): the reference's p_exact (:98-188) is a DP over
 // dp_i[u] = sum_{k=0..n2} dp_{i-1}[u-k] in wrapping uint64 followed by sequential double
@@ -19,26 +17,11 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "pvalue_math.cuh"
 
 namespace hpdex {
 
-// ---------------------------------------------------------------------------------------
-// erfc from a table. erfc is tabulated with its Taylor coefficients at x_k = k / 128,
-// 0 <= x_k < 26.5; for x near x_k, erfc(x_k + d) = sum_n c_n(x_k) d^n with
-//     c_0 = erfc(x_k),   c_n = -(2/sqrt(pi)) exp(-x_k^2) (-1)^(n-1) H_(n-1)(x_k) / n!,
-// from erfc'(x) = -(2/sqrt(pi)) exp(-x^2) and d^m/dx^m exp(-x^2) = (-1)^m H_m(x) exp(-x^2),
-// with the physicists' Hermite polynomials H_0 = 1, H_1 = 2x, H_(m+1) = 2x H_m - 2m H_(m-1).
-// With |d| <= 1/256 the n-th term is about (2 x d)^n / n! of c_0, so 13 terms leave a
-// truncation below 1e-17 relative up to x = 26.5. The sum runs as a Horner polynomial in d;
-// erfc(x_k + d) / erfc(x_k) stays above exp(-0.21), so nothing cancels. The table is built
-// once per device from the CUDA math library's erfc and exp. Beyond 26.5, erfc is below
-// 1e-307 and is returned as 0 (the comparisons of p-values floor at 1e-300); for x < 0,
-// erfc(x) = 2 - erfc(-x).
-// ---------------------------------------------------------------------------------------
-constexpr int kErfcPerUnit = 128;
-constexpr int kErfcTerms = 13;
-constexpr double kErfcXMax = 26.5;
-constexpr int kErfcPoints = (int)(kErfcXMax * kErfcPerUnit) + 2;
+// erfc table of this device (see pvalue_math.cuh), built by erfc_table_kernel
 __device__ double g_erfc_table[kErfcPoints * kErfcTerms];
 
 __global__ void erfc_table_kernel() {
@@ -59,20 +42,6 @@ __global__ void erfc_table_kernel() {
     }
 }
 
-__device__ __forceinline__ double erfc_tab(double x) {
-    const double ax = fabs(x);
-    double r = 0.0;
-    if (ax < kErfcXMax) {
-        const int k = __double2int_rn(ax * kErfcPerUnit);
-        const double d = ax - (double)k * (1.0 / kErfcPerUnit);  // exact: k / 128
-        const double* c = g_erfc_table + (size_t)k * kErfcTerms;
-        r = c[kErfcTerms - 1];
-#pragma unroll
-        for (int n = kErfcTerms - 2; n >= 0; --n) r = fma(r, d, c[n]);
-    }
-    return x < 0.0 ? 2.0 - r : r;
-}
-
 // Self-check: max relative / absolute difference of erfc_tab against the math library's erfc
 // on n points spread over [-8, 27] (relative only where erfc >= 1e-300).
 __global__ void erfc_check_kernel(long long n, unsigned long long* max_rel_bits,
@@ -81,7 +50,7 @@ __global__ void erfc_check_kernel(long long n, unsigned long long* max_rel_bits,
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const double x = -8.0 + 35.0 * ((double)i + 0.5) / (double)n;
-        const double a = erfc_tab(x), b = erfc(x);
+        const double a = erfc_tab(x, g_erfc_table), b = erfc(x);
         const double e = fabs(a - b);
         ma = fmax(ma, e);
         if (b >= 1e-300) mr = fmax(mr, e / b);
@@ -89,6 +58,55 @@ __global__ void erfc_check_kernel(long long n, unsigned long long* max_rel_bits,
     // non-negative doubles order like their bit patterns
     atomicMax(max_rel_bits, (unsigned long long)__double_as_longlong(mr));
     atomicMax(max_abs_bits, (unsigned long long)__double_as_longlong(ma));
+}
+
+// Self-check of the divisions by a known reciprocal (pvalue_math.cuh) against IEEE division
+// (__ddiv_rn), bit for bit, on n generated cases; counts the mismatches. Case kinds (i % 4):
+//   0  tie sums by N (N - 1): integers below 2^53 over N in [2, 2^24]
+//   1  random doubles with exponents in [-60, 60]
+//   2  quotients next to a rounding midpoint: a = RN((q + ulp(q)/2) b)
+//   3  x / 12 for random doubles and integers
+// Kinds 0-2 also check a / 12.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {  // splitmix64
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+__device__ __forceinline__ double rand_double(unsigned long long r, int emin, int span) {
+    const long long e = 1023 + emin + (long long)((r >> 52) % (unsigned long long)span);
+    return __longlong_as_double((long long)((unsigned long long)e << 52 | (r & 0xfffffffffffffull)));
+}
+__global__ void division_check_kernel(long long n, unsigned long long seed,
+                                      unsigned long long* mismatches) {
+    unsigned long long bad = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r1 = mix64(seed ^ (unsigned long long)i * 4u);
+        const unsigned long long r2 = mix64(r1 + 1u);
+        const int kind = (int)(i & 3);
+        double a, b;
+        if (kind == 0) {
+            a = (double)(r1 >> (11 + (r2 >> 58) % 53));  // integers of 1..53 bits
+            const double N = (double)(2 + (long long)((r2 >> 20) % (1u << 24)));
+            b = __dmul_rn(N, __dsub_rn(N, 1.0));
+        } else if (kind == 1 || kind == 3) {
+            a = rand_double(r1, -60, 121);
+            b = rand_double(r2, -60, 121);
+            if (kind == 3 && (r2 & 1u)) a = (double)(r1 >> 11);
+        } else {
+            const double q = rand_double(r1, -30, 61);
+            b = rand_double(r2, -30, 61);
+            const double half_ulp = __dsub_rn(__longlong_as_double(__double_as_longlong(q) + 1), q) * 0.5;
+            a = __fma_rn(q, b, __dmul_rn(half_ulp, b));
+        }
+        if (kind != 3) {
+            const double y = __drcp_rn(b);
+            if (__double_as_longlong(div_by_recip(a, b, y)) != __double_as_longlong(__ddiv_rn(a, b))) ++bad;
+        }
+        if (__double_as_longlong(div12(a)) != __double_as_longlong(__ddiv_rn(a, 12.0))) ++bad;
+    }
+    if (bad) atomicAdd(mismatches, bad);
 }
 
 struct PArgs {
@@ -102,6 +120,7 @@ struct PArgs {
     const long long* group_rows;
     const uint32_t* n1g;       // zero_handling = none: per gene
     const uint32_t* n2t;       // zero_handling = none: per test
+    const PConst* pk;          // zero_handling min / max / mix: per target (or null)
     int32_t zero_handling;
     int32_t alternative;
     double cc;
@@ -125,72 +144,6 @@ __device__ __forceinline__ void test_sizes(const PArgs& a, int t, int c, long lo
     }
 }
 
-// 0.70710678118654752440 rounded to double, the reference's M_SQRT1_2
-#define HPDEX_SQRT1_2 0.70710678118654752440
-
-__device__ __forceinline__ double p_asymptotic(double U1, double n1, double n2, double tie_sum,
-                                               double cc, int alt) {
-    const double N = __dadd_rn(n1, n2);
-    const double nm = __dmul_rn(n1, n2);
-    const double mu = __dmul_rn(0.5, nm);
-    double tie_term = 0.0;
-    const double denom = __dmul_rn(N, __dsub_rn(N, 1.0));
-    if (denom > 0.0) tie_term = __ddiv_rn(tie_sum, denom);
-    const double var = __ddiv_rn(__dmul_rn(nm, __dsub_rn(__dadd_rn(N, 1.0), tie_term)), 12.0);
-    const double sigma = (var > 0.0) ? __dsqrt_rn(var) : 0.0;
-    double p = 1.0;
-    if (alt == ALT_TWO_SIDED) {
-        const double U2 = __dsub_rn(nm, U1);
-        const double U = (U1 > U2 ? U1 : U2);
-        if (sigma > 0.0) {
-            const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
-            p = __dmul_rn(2.0, __dmul_rn(0.5, erfc_tab(__dmul_rn(z, HPDEX_SQRT1_2))));
-            if (p > 1.0) p = 1.0;
-            if (p < 0.0) p = 0.0;
-        }
-        return p;
-    }
-    const double U = (alt == ALT_LESS) ? __dsub_rn(nm, U1) : U1;
-    if (sigma > 0.0) {
-        const double z = __ddiv_rn(__dsub_rn(__dsub_rn(U, mu), cc), sigma);
-        p = __dmul_rn(0.5, erfc_tab(__dmul_rn(z, HPDEX_SQRT1_2)));
-    }
-    return (p < 0.0 ? 0.0 : (p > 1.0 ? 1.0 : p));
-}
-
-// fast_norm = true: the reference's scalar fast path (AI4Cell/hpdex src/cpp/include/
-// common.hpp:14-92), restated: erfc from the Chebyshev fit erfcc of Numerical Recipes (Press et
-// al., section 6.2; fractional error below 1.2e-7) with the math library's exp, mu and
-// 1/sigma as precompute_mu_inv_sd computes them, z = (|U1 - mu| - cc) / sigma two-sided,
-// (U1 - mu - cc) / sigma greater, (U1 - mu + cc) / sigma with p = 1 - sf less. (The
-// reference's vectorised variant of the same polynomial nests its terms differently, so its
-// values depend on the host's vector width; the scalar form is the one restated here.)
-__device__ __forceinline__ double erfcc_nr(double x) {
-    const double ax = fabs(x);
-    const double t = 1.0 / (1.0 + 0.5 * ax);
-    const double tau = t * exp(-ax * ax - 1.26551223 +
-                               t * (1.00002368 + t * (0.37409196 + t * (0.09678418 +
-                               t * (-0.18628806 + t * (0.27886807 + t * (-1.13520398 +
-                               t * (1.48851587 + t * (-0.82215223 + t * 0.17087277)))))))));
-    double r = (x >= 0.0) ? tau : 2.0 - tau;
-    return r < 0.0 ? 0.0 : (r > 2.0 ? 2.0 : r);
-}
-
-__device__ __forceinline__ double p_asymptotic_fast(double U1, double n1, double n2,
-                                                    double tie_sum, double cc, int alt) {
-    const double N = n1 + n2;
-    const double mu = 0.5 * n1 * n2;
-    const double denom = N * (N - 1.0);
-    const double base = n1 * n2 / 12.0;
-    const double var = (denom > 0.0) ? base * (N + 1.0 - tie_sum / denom) : n1 * n2 * (N + 1.0) / 12.0;
-    const double inv_sd = (var <= 0.0) ? 0.0 : 1.0 / sqrt(var);
-    if (inv_sd == 0.0) return 1.0;
-    const double s2 = sqrt(2.0);
-    if (alt == ALT_TWO_SIDED) return 2.0 * (0.5 * erfcc_nr(((fabs(U1 - mu) - cc) * inv_sd) / s2));
-    if (alt == ALT_GREATER) return 0.5 * erfcc_nr(((U1 - mu - cc) * inv_sd) / s2);
-    return 1.0 - 0.5 * erfcc_nr(((U1 - mu + cc) * inv_sd) / s2);
-}
-
 __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
@@ -199,8 +152,11 @@ __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
         double n1, n2;
         test_sizes(a, t, c, idx, n1, n2);
         const double u1 = a.U1[idx];
-        const double p = a.fast ? p_asymptotic_fast(u1, n1, n2, a.P[idx], a.cc, a.alternative)
-                                : p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative);
+        double p;
+        if (a.fast) p = p_asymptotic_fast(u1, n1, n2, a.P[idx], a.cc, a.alternative);
+        else if (a.pk && a.zero_handling != ZH_NONE)
+            p = p_asymptotic_k(u1, a.pk[t], a.P[idx], a.cc, a.alternative, g_erfc_table);
+        else p = p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative, g_erfc_table);
         if (a.P_out) {
             a.U1_out[idx] = u1;
             a.P_out[idx] = p;

@@ -133,6 +133,10 @@ class Plan:
     def run(self, mode: int = BATCHED) -> None:
         _lib.check(_lib.lib().hpdex_plan_run(self._h, int(mode)))
 
+    def set_fused_pvalues(self, on: bool) -> None:
+        """Asymptotic p-values inside the rank kernel (default) or in a separate kernel."""
+        _lib.check(_lib.lib().hpdex_plan_set_fused_pvalues(self._h, int(bool(on))))
+
     def download(self):
         C = self.matrix.n_cols
         U1 = np.empty((self.n_targets, C), np.float64)

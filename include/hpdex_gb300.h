@@ -72,7 +72,7 @@ typedef struct hpdex_mwu_options {
     int32_t tar_sorted;     /* accepted; see ref_sorted                                 */
     int32_t tie_correction; /* 1: use sum(t^3 - t) in the variance                      */
     int32_t use_continuity; /* 1: continuity correction 0.5                             */
-    int32_t fast_norm;      /* must be 0: the precise erfc path (see DESIGN)            */
+    int32_t fast_norm;      /* 1: the reference's fast normal tail (NR erfcc)           */
     int32_t zero_handling;  /* HPDEX_ZERO_*                                             */
     int32_t alternative;    /* HPDEX_LESS / GREATER / TWO_SIDED                         */
     int32_t method;         /* HPDEX_EXACT / HPDEX_ASYMPTOTIC                           */
@@ -109,6 +109,12 @@ int hpdex_fold_change(const double* means, int64_t n_genes, int64_t n_groups, do
  * on n_points points spread over [-8, 27]: the largest relative difference (where erfc >=
  * 1e-300) and the largest absolute difference. */
 int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_err);
+
+/* Self-check of the p-value stage's divisions by a precomputed reciprocal (Markstein's
+ * correction steps) against IEEE division, bit for bit, on n_cases generated quotients (tie
+ * sums over N (N - 1), random doubles, quotients next to a rounding midpoint, x / 12):
+ * *mismatches = the number that differ (0 expected). */
+int hpdex_selftest_division(int64_t n_cases, uint64_t seed, int64_t* mismatches);
 
 /* ---- one-shot calls (reference semantics; host pointers in and out) ---- */
 
@@ -165,12 +171,18 @@ int hpdex_plan_destroy(hpdex_plan* p);
 #define HPDEX_MODE_PLAIN 1
 int hpdex_plan_run(hpdex_plan* p, int32_t mode);
 
+/* Asymptotic plans compute their p-values inside the rank kernel (on = 1, the default):
+ * each gene's tests are finished by a few warps during the next gene's rank phase, so the
+ * FP64 work overlaps the integer work. on = 0 runs a separate p-value kernel after the rank
+ * kernel instead; the results are the same. Exact plans accept only on = 0. */
+int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on);
+
 /* Copies U1 / P (n_targets x n_cols, target-major) to host; either pointer may be NULL. */
 int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
 
 /* Device times (ms, CUDA events on the launching stream) of the last hpdex_plan_run:
- * [0] whole run, [1] rank kernel(s), [2] p-value kernel; and the number of kernel
- * launches it made. */
+ * [0] whole run, [1] rank kernel(s) (with the p-values when fused), [2] p-value kernel
+ * (0 when fused); and the number of kernel launches it made. */
 int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches);
 
 /* ---- no-allocation variant (no counterpart in the reference) ----

@@ -127,6 +127,17 @@ def test_erfc_table_against_math_library():
     assert ab.value <= 1e-15, ab.value
 
 
+def test_divisions_by_known_reciprocal_equal_ieee_division():
+    """The p-value stage divides tie sums by N (N - 1) with a precomputed reciprocal and
+    variances by 12 with RN(1/12), plus Markstein's correction steps (pvalue_math.cuh); both must
+    give IEEE division's double on 2^30 generated quotients, midpoint-adjacent ones included."""
+    import ctypes
+    from hpdex_gb300 import _lib
+    bad = ctypes.c_int64(-1)
+    _lib.check(_lib.lib().hpdex_selftest_division(1 << 30, 12345, ctypes.byref(bad)))
+    assert bad.value == 0, bad.value
+
+
 @pytest.mark.parametrize("alt", [0, 1, 2])
 def test_fast_norm_matches_restated_reference_fast_path(alt):
     """fast_norm=True: the reference's scalar fast normal tail (Numerical Recipes erfcc), here
