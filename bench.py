@@ -222,6 +222,8 @@ def run_ours(args, rank, world):
     tests = T * C
     M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
     plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
+    if args.only_batched and args.separate_pvalues:
+        plan.set_fused_pvalues(False)
     for _ in range(max(3, args.warmup)):
         plan.run(BATCHED)
     U1, P = plan.download()
@@ -286,12 +288,14 @@ def run_ours(args, rank, world):
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T, tie_correction=True,
                         use_continuity=True, zero_handling=1, fast_norm=False)  # warm-up
-    te = time.perf_counter()
+    e2e_calls = []
     for _ in range(e2e_steps):
+        te = time.perf_counter()
         U1e, Pe = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T,
                                       tie_correction=True, use_continuity=True, zero_handling=1,
                                       fast_norm=False)
-    e2e_wall = (time.perf_counter() - te) / e2e_steps
+        e2e_calls.append(time.perf_counter() - te)
+    e2e_wall = sum(e2e_calls) / e2e_steps
     same = same and bool(np.array_equal(U1e, U1) and np.array_equal(Pe, P))
 
     serving = serving_leg(M, w) if not args.no_serving else None
@@ -315,6 +319,8 @@ def run_ours(args, rank, world):
                    "wall_ms_per_step": wall / args.steps * 1e3},
         "e2e": {"value": world * tests / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_wall * 1e3,
+                "calls": e2e_steps, "median_ms": statistics.median(e2e_calls) * 1e3,
+                "min_ms": min(e2e_calls) * 1e3, "max_ms": max(e2e_calls) * 1e3,
                 "call": "hpdex_gb300.backend.bin.kernel.mannwhitneyu (host numpy in/out, "
                         "fast_norm=False as the reference wrapper passes it)"},
         "plain": {"value": tests / (ptot / 1e3), "unit": UNIT, "ms_per_step": ptot,
@@ -350,11 +356,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-genes", type=int, default=800)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched form only (no plain form, e2e or CPU legs); for ncu")
+    ap.add_argument("--separate-pvalues", action="store_true",
+                    help="with --only-batched: p-values in a separate kernel (for ncu)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
