@@ -61,18 +61,23 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per rank-kernel launch from the committed ncu summary, if present."""
+def profile_figure(key):
+    """A per-launch figure of the rank kernel from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "mwu_rank_kernel_perturb_screen.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("traffic_bytes_per_launch_full_workload:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
                 return None
     return None
+
+
+def traffic_from_profile():
+    """DRAM bytes per rank-kernel launch (dram__bytes_read.sum + dram__bytes_write.sum)."""
+    return profile_figure("traffic_bytes_per_launch_full_workload")
 
 
 class ClockSampler:
@@ -305,6 +310,20 @@ def run_ours(args, rank, world):
     rank_avg = statistics.mean(rank_ms) / 1e3
     achieved = B / rank_avg / 1e9
     traffic = traffic_from_profile()
+    # the kernel is issue-bound: warp instructions per launch (ncu smsp__inst_executed.sum)
+    # over the event time, against 4 issue slots per SM per cycle at the sampled SM clock
+    inst = profile_figure("warp_instructions_per_launch_full_workload")
+    issue = None
+    if inst and clocks.get("sm_mhz"):
+        import ctypes
+        from hpdex_gb300 import _lib
+        sms = ctypes.c_int32()
+        _lib.check(_lib.lib().hpdex_device_sm_count(ctypes.byref(sms)))
+        issue_peak = 4 * sms.value * clocks["sm_mhz"] * 1e6
+        issue = {"achieved": inst / rank_avg, "peak": issue_peak, "unit": "warp inst/s",
+                 "frac": inst / rank_avg / issue_peak,
+                 "note": "ncu smsp__inst_executed.sum per launch / event time; "
+                         "peak = 4 sub-partitions x SMs x sampled SM clock"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -336,7 +355,8 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
                      "kernel": "mwu_rank_kernel", "algorithmic_bytes": B,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "issue": issue},
         "clocks": clocks,
         "gpu_launches": launches,
     }

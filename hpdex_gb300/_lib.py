@@ -42,6 +42,7 @@ EXPORTS = {
     "hpdex_mwu_options_default": (None, [ctypes.POINTER(MwuOptions)]),
     "hpdex_last_error": (ctypes.c_char_p, []),
     "hpdex_device_count": (ctypes.c_int, []),
+    "hpdex_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
     "hpdex_release_cached_memory": (ctypes.c_int, []),
     "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),

@@ -951,6 +951,14 @@ int hpdex_device_count(void) {
     return n;
 }
 
+int hpdex_device_sm_count(int32_t* sms) {
+    if (!sms) return fail(HPDEX_ERR_ARGUMENT, "sms is NULL");
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    *sms = dev.sms;
+    return HPDEX_OK;
+}
+
 int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
                         const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
                         hpdex_matrix** out) {

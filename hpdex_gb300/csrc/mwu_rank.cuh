@@ -713,6 +713,13 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi, s_wdone;
     __shared__ int s_pv_gene, s_pv_task;  // gene whose p-values are pending (-1: none)
     __shared__ uint32_t s_pvq;            // its p-value tiles taken so far
+    // the next gene and its column metadata, fetched during the current gene's finalize by a
+    // thread that has no target to finalize, so that the work-queue atomic and the dependent
+    // loads are off the critical path
+    __shared__ int s_next_gene, s_next_task;
+    __shared__ long long s_next_p0, s_next_p1;
+    __shared__ unsigned long long s_next_kmin, s_next_kmax;
+    __shared__ uint32_t s_next_hz;
     __shared__ uint32_t s_wsx[32], s_wsy[32];
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
@@ -771,25 +778,40 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         s_pv_gene = -1; s_pv_task = 0; s_pvq = 0u;
     }
 
-    bool first = true;
+    bool first = true;  // (thread NT - 1) the plain form's one gene is still to be handed out
+    auto fetch_next = [&]() {
+        int c = -1, ti = 0;
+        if (a.single_gene >= 0) {
+            c = first ? a.single_gene : -1;
+            first = false;
+        } else {
+            const int gi = atomicAdd(a.queue, 1);
+            if (gi < a.n_order) {
+                c = a.order[gi];
+                ti = a.order_task ? (int)a.order_task[gi] : 0;
+            }
+        }
+        s_next_gene = c;
+        s_next_task = ti;
+        if (c >= 0) {
+            const RankTask* t = a.tasks + ti;
+            s_next_p0 = t->indptr[c];
+            s_next_p1 = t->indptr[c + 1];
+            s_next_kmin = t->col_kmin[c];
+            s_next_kmax = t->col_kmax[c];
+            s_next_hz = t->col_has_zero[c];
+        }
+    };
+    if (tid == NT - 1) fetch_next();
+    __syncthreads();
+
     for (;;) {
         if (tid == 0) {
-            int c = -1, ti = 0;
-            if (a.single_gene >= 0) {
-                c = first ? a.single_gene : -1;
-            } else {
-                const int gi = atomicAdd(a.queue, 1);
-                if (gi < a.n_order) {
-                    c = a.order[gi];
-                    ti = a.order_task ? (int)a.order_task[gi] : 0;
-                }
-            }
-            s_gene = c;
-            s_task = ti;
+            s_gene = s_next_gene;
+            s_task = s_next_task;
             s_tref = 0ull;
             s_maxb = 0u;
         }
-        first = false;
         for (int g = tid; g < GL; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
         __syncthreads();
         const int c = s_gene;
@@ -803,8 +825,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         const int G = tk->G, zh = tk->zero_handling;
         const GT* gidp = reinterpret_cast<const GT*>(tk->group_of_row);
         const uint32_t nrows = (uint32_t)tk->n_rows;
-        const long long p0 = tk->indptr[c];
-        const uint32_t nraw = (uint32_t)(tk->indptr[c + 1] - p0);
+        const long long p0 = s_next_p0;
+        const uint32_t nraw = (uint32_t)(s_next_p1 - p0);
         // entries of this gene, re-based: entry i is rows[i], data[i]; its decoded copy is
         // dk/dg[i]. Passes over the entries go by warp tiles of 128: lane l of a warp takes
         // entries t + l + 32k (k < 4), so that neighbouring lanes read neighbouring entries
@@ -813,8 +835,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         const V* data = reinterpret_cast<const V*>(tk->data) + p0;
 
         // ---- bucket function from the column's key range ----
-        K kmin = (K)tk->col_kmin[c], kmax = (K)tk->col_kmax[c];
-        if (zh == ZH_NONE && tk->col_has_zero[c]) {
+        K kmin = (K)s_next_kmin, kmax = (K)s_next_kmax;
+        if (zh == ZH_NONE && s_next_hz) {
             const K kz = Val<V>::key(V(0));
             kmin = kz < kmin ? kz : kmin;
             kmax = kz > kmax ? kz : kmax;
@@ -1009,6 +1031,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         __syncthreads();
 
         // ---- finalize per target ----
+        // the s_next_* values of this gene were read after the barriers above; the next gene
+        // is fetched now (thread NT - 1 finalizes a target only when G > NT)
+        if (tid == NT - 1) fetch_next();
         const unsigned long long T_ref = s_tref;
         const unsigned long long nz1 = nz[0];
         for (int g = 1 + tid; g < G; g += NT) {

@@ -89,6 +89,9 @@ const char* hpdex_last_error(void);
 /* Number of visible CUDA devices (0 when none); never fails. */
 int hpdex_device_count(void);
 
+/* Streaming multiprocessors of the current device (152 on a GB300). */
+int hpdex_device_sm_count(int32_t* sms);
+
 /* Device memory of destroyed matrices, plans and finished one-shot calls stays cached for
  * reuse by later calls (no cudaMalloc/cudaFree per call); this returns it to the driver. */
 int hpdex_release_cached_memory(void);
