@@ -44,6 +44,8 @@ EXPORTS = {
     "hpdex_device_count": (ctypes.c_int, []),
     "hpdex_device_sm_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int32)]),
     "hpdex_release_cached_memory": (ctypes.c_int, []),
+    "hpdex_host_buffer_acquire": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_host_buffer_release": (ctypes.c_int, [ctypes.c_void_p]),
     "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
     "hpdex_selftest_division": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64,
@@ -137,8 +139,41 @@ def device_count() -> int:
 
 
 def release_cached_memory() -> None:
-    """Return the device memory that finished calls keep cached for reuse to the driver."""
+    """Return the device memory (and idle page-locked result buffers) that finished calls keep
+    cached for reuse to the driver."""
     check(lib().hpdex_release_cached_memory())
+
+
+_PINNED_TYPES = {}
+
+
+def _pinned_release(self):
+    try:
+        lib().hpdex_host_buffer_release(ctypes.addressof(self))
+    except Exception:  # interpreter shutdown
+        pass
+
+
+def result_array(shape):
+    """A float64 array for results: backed by a page-locked buffer from the library's pool when
+    one is available (the device then writes it directly; the buffer goes back to the pool
+    when the array and its views are gone), else ordinary memory."""
+    import numpy as np
+    n = 1
+    for d in shape:
+        n *= int(d)
+    nbytes = 8 * n
+    if nbytes == 0:
+        return np.empty(shape, np.float64)
+    ptr = ctypes.c_void_p()
+    if lib().hpdex_host_buffer_acquire(nbytes, ctypes.byref(ptr)) != 0 or not ptr.value:
+        return np.empty(shape, np.float64)
+    T = _PINNED_TYPES.get(nbytes)
+    if T is None:
+        T = type("PinnedBuffer", (ctypes.c_char * nbytes,), {"__del__": _pinned_release})
+        _PINNED_TYPES[nbytes] = T
+    buf = T.from_address(ptr.value)
+    return np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape)
 
 
 def bh_fdr(p):

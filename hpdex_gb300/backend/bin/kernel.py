@@ -88,8 +88,8 @@ def mannwhitneyu(data, indices, indptr, group_id, n_targets, ref_sorted=False, t
         raise RuntimeError("indices is shorter than data")
     opt = _options(ref_sorted, tar_sorted, tie_correction, use_continuity, fast_norm,
                    zero_handling, alternative, method, exact_variant)
-    U1 = np.empty((max(n_targets, 0), C), np.float64)
-    P = np.empty((max(n_targets, 0), C), np.float64)
+    U1 = _lib.result_array((max(n_targets, 0), C))
+    P = _lib.result_array((max(n_targets, 0), C))
     t0 = time.perf_counter()
     st = _lib.lib().hpdex_mannwhitneyu(_DTYPES[data.dtype], data.ctypes.data, indices.ctypes.data,
                                        indptr.ctypes.data, R, C, nnz, group_id.ctypes.data,

@@ -226,6 +226,71 @@ MemCache& mem_cache() {
     return *c;
 }
 
+// Page-locked host buffers for result arrays. The Python wrapper of the one-shot call takes one
+// per output array: the device writes the results straight into it, with no pages to fault in
+// first, and the buffer comes back when the array is released. A released buffer is handed out
+// again to a request of at most its size and at least half of it; at most kHeldBytes are held
+// (idle or lent out), beyond which a request gets NULL and the caller uses ordinary memory.
+class HostPool {
+    std::mutex mu_;
+    std::multimap<size_t, void*> idle_;
+    std::map<void*, size_t> live_;
+    size_t held_ = 0;
+
+  public:
+    static constexpr size_t kHeldBytes = size_t(2) << 30;
+    void* get(size_t bytes) {
+        const size_t g = bytes >= (size_t(32) << 20) ? (size_t(2) << 20) : (size_t(64) << 10);
+        const size_t want = (bytes + g - 1) / g * g;
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            auto it = idle_.lower_bound(want);
+            if (it != idle_.end() && it->first / 2 <= want) {
+                void* p = it->second;
+                live_[p] = it->first;
+                idle_.erase(it);
+                return p;
+            }
+            if (held_ + want > kHeldBytes) return nullptr;
+            held_ += want;  // reserved while allocating
+        }
+        void* p = nullptr;
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocPortable | cudaHostAllocMapped);
+        void* dp = nullptr;
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&dp, p, 0);
+        if (e != cudaSuccess || dp != p) {  // the device must see the buffer at its host address
+            cudaGetLastError();
+            if (p) cudaFreeHost(p);
+            std::lock_guard<std::mutex> lock(mu_);
+            held_ -= want;
+            return nullptr;
+        }
+        std::lock_guard<std::mutex> lock(mu_);
+        live_[p] = want;
+        return p;
+    }
+    bool put(void* p) {
+        std::lock_guard<std::mutex> lock(mu_);
+        auto it = live_.find(p);
+        if (it == live_.end()) return false;
+        idle_.insert({it->second, p});
+        live_.erase(it);
+        return true;
+    }
+    void release_idle() {
+        std::lock_guard<std::mutex> lock(mu_);
+        for (auto& kv : idle_) {
+            cudaFreeHost(kv.second);
+            held_ -= kv.first;
+        }
+        idle_.clear();
+    }
+};
+HostPool& host_pool() {
+    static HostPool* h = new HostPool();
+    return *h;
+}
+
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -939,6 +1004,19 @@ int hpdex_fold_change(const double* means, int64_t n_genes, int64_t n_groups, do
 
 int hpdex_release_cached_memory(void) {
     mem_cache().release_all();
+    host_pool().release_idle();
+    return HPDEX_OK;
+}
+
+int hpdex_host_buffer_acquire(int64_t bytes, void** ptr) {
+    if (!ptr || bytes < 0) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    *ptr = bytes > 0 ? host_pool().get((size_t)bytes) : nullptr;
+    return HPDEX_OK;
+}
+
+int hpdex_host_buffer_release(void* ptr) {
+    if (!ptr) return HPDEX_OK;
+    if (!host_pool().put(ptr)) return fail(HPDEX_ERR_ARGUMENT, "not a buffer of hpdex_host_buffer_acquire");
     return HPDEX_OK;
 }
 
@@ -1434,13 +1512,23 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     // Output pages never written before (fresh numpy arrays) would fault one by one when the
     // device writes them; a host thread touches them while the first chunks are in flight, and
     // the compute stream waits for it before the first p-value kernel.
-    const bool direct = m->dev.pageable_access && U1_out && P_out;
-    std::atomic<int> touched{0};
+    // Page-locked outputs (hpdex_host_buffer_acquire) are written directly on any system and
+    // need no touching; pageable ones directly where the device can reach pageable memory.
+    bool pinned_out = false;
+    if (U1_out && P_out) {
+        cudaPointerAttributes a1{}, a2{};
+        if (cudaPointerGetAttributes(&a1, U1_out) == cudaSuccess &&
+            cudaPointerGetAttributes(&a2, P_out) == cudaSuccess)
+            pinned_out = a1.type == cudaMemoryTypeHost && a2.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+    }
+    const bool direct = (m->dev.pageable_access || pinned_out) && U1_out && P_out;
+    std::atomic<int> touched{pinned_out ? 1 : 0};
     struct Toucher {
         std::thread t;
         ~Toucher() { if (t.joinable()) t.join(); }
     } toucher;
-    if (direct) {
+    if (direct && !pinned_out) {
         const size_t bytes = sizeof(double) * (size_t)(T * C);
         toucher.t = std::thread([U1_out, P_out, bytes, &touched] {
             for (size_t o = 0; o < bytes; o += 4096) {
@@ -1504,7 +1592,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         pa.alternative = opt->alternative;
         pa.cc = opt->use_continuity ? 0.5 : 0.0;
         pa.fast = opt->fast_norm;
-        if (direct && j == 0) {
+        if (direct && !pinned_out && j == 0) {
             CUDA_TRY(cudaLaunchHostFunc(sc, [](void* f) {
                 const auto* done = static_cast<const std::atomic<int>*>(f);
                 while (!done->load(std::memory_order_acquire)) std::this_thread::yield();

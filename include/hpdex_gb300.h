@@ -96,6 +96,14 @@ int hpdex_device_sm_count(int32_t* sms);
  * reuse by later calls (no cudaMalloc/cudaFree per call); this returns it to the driver. */
 int hpdex_release_cached_memory(void);
 
+/* Page-locked host buffers for result arrays (the Python wrapper uses them for U1 / P): the
+ * one-shot call writes results into such buffers directly, with no host pages to fault in.
+ * acquire sets *ptr to a buffer of at least `bytes` bytes, or to NULL when the pool (2 GiB
+ * held at most) cannot lend one: use ordinary memory then. release returns a buffer to the
+ * pool; hpdex_release_cached_memory frees the idle ones. */
+int hpdex_host_buffer_acquire(int64_t bytes, void** ptr);
+int hpdex_host_buffer_release(void* ptr);
+
 /* ---- DE post-processing on the device (the reference DE driver does these on the host,
  * de.py:138-142 and :174-184) ----
  * hpdex_bh_fdr: Benjamini-Hochberg adjusted p-values of p[0..n), as

@@ -52,3 +52,27 @@ def test_oneshot_dtypes_equal_resident(dtype):
                                 zero_handling=1, fast_norm=False)
     np.testing.assert_array_equal(U1, U1r)
     np.testing.assert_array_equal(P, Pr)
+
+
+def test_results_in_pooled_page_locked_buffers():
+    """The wrapper's result arrays come from the library's page-locked buffer pool: released
+    with the arrays, reused by the next call, never shared with a result still alive."""
+    import hpdex_gb300
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.umi_counts(seed=6, n_rows=6_000, n_cols=150, n_targets=9)
+    hpdex_gb300.release_cached_memory()  # no idle buffers left over from earlier tests
+    call = lambda: kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                       zero_handling=1, fast_norm=False)
+    a = call()
+    assert type(a[0].base.base).__name__ == "PinnedBuffer"
+    addr = {a[0].ctypes.data, a[1].ctypes.data}
+    ref = (a[0].copy(), a[1].copy())
+    del a
+    b = call()
+    assert {b[0].ctypes.data, b[1].ctypes.data} == addr  # the released buffers were reused
+    c = call()  # b is alive: c gets other buffers, and b keeps its values
+    assert not ({c[0].ctypes.data, c[1].ctypes.data} & addr)
+    for U1, P in (b, c):
+        np.testing.assert_array_equal(U1, ref[0])
+        np.testing.assert_array_equal(P, ref[1])
