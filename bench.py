@@ -81,9 +81,10 @@ def traffic_from_profile():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling while the timed region runs."""
+    """nvidia-smi clock/throttle sampling (every 50 ms); stop() keeps the samples taken inside
+    the timed region (wall-clock window) and says how many there were."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -92,12 +93,35 @@ class ClockSampler:
         self.p = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, ValueError):
             self.p = None
 
-    def stop(self):
+    def wait_first(self, timeout=3.0):
+        """Returns once nvidia-smi has written a sample (so that sampling covers what follows)."""
+        t_end = time.time() + timeout
+        while self.p is not None and time.time() < t_end:
+            try:
+                if os.path.getsize(self.f.name) > 0:
+                    return
+            except OSError:
+                return
+            time.sleep(0.01)
+
+    @staticmethod
+    def _parse(line):
+        import datetime
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 10:
+            return None
+        try:
+            t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+        return t, parts[1:]
+
+    def stop(self, t_begin=None, t_end=None):
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -109,18 +133,25 @@ class ClockSampler:
         rows = []
         with open(self.f.name) as fh:
             for line in fh:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
+                r = self._parse(line)
+                if r is not None:
+                    rows.append(r)
         os.unlink(self.f.name)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = [r for t, r in rows if t_begin is None or (t_begin <= t <= t_end)]
+        if inside:
+            use, where = inside, "inside the timed region"
+        else:  # a timed region shorter than the sampling period: the sample nearest to it
+            mid = 0.5 * (t_begin + t_end)
+            use, where = [min(rows, key=lambda tr: abs(tr[0] - mid))[1]], "nearest to the timed region"
+        sm = [float(r[1]) for r in use if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in use if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in use for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(use), "where": where}
 
 
 def make_workload(args, rank):
@@ -229,6 +260,7 @@ def run_ours(args, rank, world):
     plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
     if args.only_batched and args.separate_pvalues:
         plan.set_fused_pvalues(False)
+    sampler = ClockSampler(0)  # sampling from before the warm-up on
     for _ in range(max(3, args.warmup)):
         plan.run(BATCHED)
     U1, P = plan.download()
@@ -238,7 +270,8 @@ def run_ours(args, rank, world):
         import torch.distributed as dist  # host-side barrier / max only
         dist.init_process_group("gloo")
         dist.barrier()
-    sampler = ClockSampler(0)
+    sampler.wait_first()
+    tw0 = time.time()
     t0 = time.perf_counter()
     dev_ms, rank_ms, p_ms, launches = [], [], [], 0
     for _ in range(args.steps):
@@ -249,7 +282,7 @@ def run_ours(args, rank, world):
         p_ms.append(pv)
         launches += nl
     wall = time.perf_counter() - t0
-    clocks = sampler.stop()
+    clocks = sampler.stop(tw0, time.time())
     elapsed_dev = sum(dev_ms) / 1e3
     if dist is not None:
         import torch
@@ -373,7 +406,9 @@ def run_ours(args, rank, world):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 300 for ours: about 1 s, so that the 50 ms clock "
+                         "samples fall inside the timed region; 3 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -384,6 +419,8 @@ def main():
     ap.add_argument("--separate-pvalues", action="store_true",
                     help="with --only-batched: p-values in a separate kernel (for ncu)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 3 if args.impl == "reference" else 300
     rank, world, local = dist_env()
     if world > 1:
         # one process per GPU: each rank sees only its own device (independent replicas)
