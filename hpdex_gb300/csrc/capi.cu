@@ -1800,11 +1800,18 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
     }
     CUDA_TRY(cudaMemsetAsync(b.queue.p, 0, sizeof(int32_t), st));
 
-    // pages of the caller's output arrays that were never written fault one by one when the
-    // device writes them: touch them here
+    // results go straight into the caller's arrays when they are page-locked (result buffers
+    // of hpdex_host_buffer_acquire) or when the device reaches pageable memory; pageable pages
+    // that were never written would fault one by one when the device writes them: touch them
     for (ServerQuery* q : b.q) {
-        q->direct = S->dev.pageable_access;
-        if (!q->direct) continue;
+        bool pinned = false;
+        cudaPointerAttributes a1{}, a2{};
+        if (cudaPointerGetAttributes(&a1, q->U1_out) == cudaSuccess &&
+            cudaPointerGetAttributes(&a2, q->P_out) == cudaSuccess)
+            pinned = a1.type == cudaMemoryTypeHost && a2.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        q->direct = pinned || S->dev.pageable_access;
+        if (!q->direct || pinned) continue;
         const size_t bytes = sizeof(double) * (size_t)(q->T * S->mats[(size_t)q->matrix]->n_cols);
         for (size_t o = 0; o < bytes; o += 4096) {
             reinterpret_cast<volatile unsigned char*>(q->U1_out)[o] = 0;

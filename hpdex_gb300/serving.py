@@ -71,8 +71,8 @@ class Server:
         if gid.size != m.n_rows:
             raise ValueError(f"group_id has {gid.size} entries, the matrix {m.n_rows} rows")
         T = int(n_targets)
-        U1 = np.empty((max(T, 0), m.n_cols), np.float64)
-        P = np.empty((max(T, 0), m.n_cols), np.float64)
+        U1 = _lib.result_array((max(T, 0), m.n_cols))
+        P = _lib.result_array((max(T, 0), m.n_cols))
         qid = ctypes.c_int64()
         opt = make_options(**options)
         _lib.check(_lib.lib().hpdex_server_submit(self._h, int(matrix_id), gid.ctypes.data, T,
