@@ -1418,13 +1418,13 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     TRY(m->col_kmin.alloc(std::max<long long>(C, 1)));
     TRY(m->col_kmax.alloc(std::max<long long>(C, 1)));
     TRY(m->col_has_zero.alloc(std::max<long long>(C, 1)));
-    CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t) * ((size_t)C + 1), cudaMemcpyHostToDevice));
     m->col_nnz.resize((size_t)C);
     for (long long c = 0; c < C; ++c) {
         m->col_nnz[(size_t)c] = indptr[c + 1] - indptr[c];
         m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
     }
     if (C == 0) {
+        CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t), cudaMemcpyHostToDevice));
         hpdex_plan* praw = nullptr;
         TRY(plan_create(m.get(), group_id, n_targets, opt, &praw, false));
         delete praw;
@@ -1444,13 +1444,10 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     const int K = (int)cb.size() - 1;
     std::vector<long long> longest((size_t)K, 0);
     long long max_chunk = 0;
-    std::vector<int32_t> order((size_t)C);
     for (int k = 0; k < K; ++k) {
         max_chunk = std::max<long long>(max_chunk, (long long)(indptr[cb[k + 1]] - indptr[cb[k]]));
-        auto b = order.begin() + cb[k], e = order.begin() + cb[k + 1];
-        std::iota(b, e, (int32_t)cb[k]);
-        std::stable_sort(b, e, [&](int32_t x, int32_t y) { return m->col_nnz[(size_t)x] > m->col_nnz[(size_t)y]; });
-        longest[(size_t)k] = m->col_nnz[(size_t)*b];
+        for (long long c = cb[k]; c < cb[k + 1]; ++c)
+            longest[(size_t)k] = std::max(longest[(size_t)k], m->col_nnz[(size_t)c]);
     }
     std::vector<int> seq((size_t)K);
     std::iota(seq.begin(), seq.end(), 0);
@@ -1497,7 +1494,17 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         plan_status = plan_create(m.get(), group_id, n_targets, opt, &praw, false);
         if (plan_status != HPDEX_OK) plan_error = hpdex_last_error();
     });
-    const int first_copy = enqueue_copy(0);
+    // column pointers, then the first chunk; the per-chunk gene order while they upload
+    int first_copy = HPDEX_OK;
+    if (cudaMemcpyAsync(m->indptr.p, indptr, sizeof(int64_t) * ((size_t)C + 1), cudaMemcpyHostToDevice, sx) != cudaSuccess)
+        first_copy = fail(HPDEX_ERR_CUDA, "column pointer upload failed");
+    if (first_copy == HPDEX_OK) first_copy = enqueue_copy(0);
+    std::vector<int32_t> order((size_t)C);  // each chunk's columns longest first
+    for (int k = 0; k < K; ++k) {
+        auto ob = order.begin() + cb[k], oe = order.begin() + cb[k + 1];
+        std::iota(ob, oe, (int32_t)cb[k]);
+        std::stable_sort(ob, oe, [&](int32_t x, int32_t y) { return m->col_nnz[(size_t)x] > m->col_nnz[(size_t)y]; });
+    }
     planner.join();
     std::unique_ptr<hpdex_plan> p(praw);
     if (plan_status != HPDEX_OK) return fail(plan_status, "%s", plan_error.c_str());
