@@ -117,8 +117,10 @@ constexpr int kMaxRunsByMin = 24;  // distinct keys extracted by warp minimum pe
 constexpr uint32_t kInvalid = 0xffffffffu;
 constexpr uint32_t kTaken = 0xfffffffeu;    // a big-list entry that a warp has resolved
 constexpr int kDrainWaitIters = 4096;       // polls (with a short sleep) for a big-list entry
-constexpr int kPvWarps = 8;                 // warps (two per SM sub-partition) that take a
-                                            // gene's p-value tiles in the next gene's rank phase
+constexpr int kPvWarps = 4;                 // warps (one per SM sub-partition) that take a
+                                            // gene's p-value tiles at the start of the next
+                                            // gene's rank phase; warps waiting in its drain
+                                            // take further tiles
 // Group ids inside the kernel: 16-bit when the accumulators are in shared memory (which
 // bounds G far below 65535), else 32-bit; all ones marks an entry outside every group.
 template <bool ACC_SMEM>
@@ -518,10 +520,11 @@ __device__ void resolve_big(uint32_t s0, uint32_t m, uint32_t rb, const EK* ek, 
 
 // ---------------------------------------------------------------------------------------
 // Fused p-values. A gene's finalize writes U1 and the tie sum of its tests; the FP64 work of
-// turning them into p-values is left pending and done during the next gene's rank phase by
-// kPvWarps warps, while the other warps keep the integer pipes busy (FP64 is the scarce pipe
-// on GB300, and the rank phase hardly uses it). The CTA's last gene is finished by all warps
-// after the work queue runs dry.
+// turning them into p-values is left pending and done during the next gene's rank phase, by
+// kPvWarps warps at its start and by warps that would otherwise wait in its drain, while the
+// other warps keep the integer pipes busy (FP64 is the scarce pipe on GB300, and the rank phase
+// hardly uses it). Tiles still pending before the finalize are taken by all warps; the CTA's
+// last gene is finished by all warps after the work queue runs dry.
 // ---------------------------------------------------------------------------------------
 // Tests of targets 1 + 32q + lane of gene c: P replaces the tie sum. Not inlined, so that the
 // FP64 arithmetic's registers stay out of the rank loops' allocation (one test per lane: more
@@ -667,7 +670,19 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
     __syncwarp();
     if (lane == 0) atomicAdd(s_wdone, 1u);
     const uint32_t nwarps = blockDim.x >> 5;
+    const uint32_t pv_ntiles = pv_tk ? ((uint32_t)pv_tk->G + 30u) / 32u : 0u;
     for (;;) {
+        if (pv_tk) {  // no listed bucket to take yet while chunks still run: a p-value tile instead
+            uint32_t q = 0xffffffffu;
+            if (lane == 0 && *(volatile uint32_t*)s_bigi >= min(*(volatile uint32_t*)s_nbig, biglist_cap) &&
+                *(volatile uint32_t*)s_wdone < nwarps && *(volatile uint32_t*)s_pvq < pv_ntiles)
+                q = atomicAdd(s_pvq, 1u);
+            q = __shfl_sync(0xffffffffu, q, 0);
+            if (q < pv_ntiles) {
+                pvalue_tile(pv_tk, pv_c, q, erfc_table);
+                continue;
+            }
+        }
         uint32_t b = kInvalid, st = 0;  // st: 0 a bucket, 1 list exhausted, 2 wait ran out
         if (lane == 0) {
             const uint32_t q = atomicAdd(s_bigi, 1u);
