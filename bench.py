@@ -52,6 +52,15 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(values, dist):
+    """Element-wise maximum of this rank's floats over all ranks (gloo, host side): the job's
+    time is its slowest rank's."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -285,10 +294,7 @@ def run_ours(args, rank, world):
     clocks = sampler.stop(tw0, time.time())
     elapsed_dev = sum(dev_ms) / 1e3
     if dist is not None:
-        import torch
-        t = torch.tensor([elapsed_dev, wall], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_dev, wall = float(t[0]), float(t[1])
+        elapsed_dev, wall = max_over_ranks([elapsed_dev, wall], dist)
     value = world * tests * args.steps / elapsed_dev
 
     line_core = {"value": value, "ms_per_step": statistics.mean(dev_ms),
