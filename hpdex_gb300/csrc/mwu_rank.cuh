@@ -818,6 +818,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         }
     };
     if (tid == NT - 1) fetch_next();
+    for (int b = tid; b <= NBMAX; b += NT) { hall[b] = 0u; href[b] = 0u; }
     __syncthreads();
 
     for (;;) {
@@ -864,8 +865,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             const int bl = bit_length(K(kmax - kmin));
             shift = bl > nbl ? bl - nbl : 0;
         }
-        for (int b = tid; b <= NB; b += NT) { hall[b] = 0u; href[b] = 0u; }
-        __syncthreads();
+        // (the bucket table is all zeros here: zeroed before the first gene, and each gene
+        // clears the entries it used while it finalizes)
 
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
@@ -1080,6 +1081,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             tk->U1[idx] = (double)u1x2 * 0.5;
             tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
         }
+        for (int b = tid; b <= NB; b += NT) { hall[b] = 0u; href[b] = 0u; }  // for the next gene
         if (tid == 0 && a.erfc_table) {  // this gene's p-values: pending until the next gene
             s_pv_gene = c;
             s_pv_task = s_task;
