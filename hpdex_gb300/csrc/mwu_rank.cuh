@@ -258,15 +258,16 @@ __device__ void block_scan2(uint32_t* x, uint32_t* y, int L, uint32_t* wsx, uint
     const uint32_t ix = warp_incl_scan(sx), iy = warp_incl_scan(sy);
     if (lane == 31) { wsx[warp] = ix; wsy[warp] = iy; }
     __syncthreads();
-    if (warp == 0) {
+    // every warp scans the warp totals itself (no second barrier)
+    uint32_t ox, oy;
+    {
         const uint32_t ux = lane < NT / 32 ? wsx[lane] : 0u;
         const uint32_t uy = lane < NT / 32 ? wsy[lane] : 0u;
         const uint32_t px = warp_incl_scan(ux), py = warp_incl_scan(uy);
-        if (lane < NT / 32) { wsx[lane] = px - ux; wsy[lane] = py - uy; }
-        if (lane == 31) { x[L] = px; y[L] = py; }
+        ox = __shfl_sync(0xffffffffu, px - ux, warp) + ix - sx;
+        oy = __shfl_sync(0xffffffffu, py - uy, warp) + iy - sy;
+        if (warp == 0 && lane == 31) { x[L] = px; y[L] = py; }
     }
-    __syncthreads();
-    uint32_t ox = wsx[warp] + ix - sx, oy = wsy[warp] + iy - sy;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const uint32_t tx = vx[i], ty = vy[i];
