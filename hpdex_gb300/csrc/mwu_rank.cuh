@@ -717,7 +717,9 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
         if (v != kTaken && v != kInvalid) resolve_listed(v);
     }
     __syncthreads();
+    // ready for the next slab (whose scatter barrier orders these before its rank phase)
     for (uint32_t q = threadIdx.x; q < nbig; q += blockDim.x) biglist[q] = kInvalid;
+    if (threadIdx.x == 0) { *s_chunk = 0u; *s_nbig = 0u; *s_bigi = 0u; *s_wdone = 0u; }
 }
 
 template <class V, int NT, bool ACC_SMEM>
@@ -946,23 +948,26 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         // bucket) and buckets of later slabs still hold their starts.
         unsigned long long tref = 0ull;
         uint32_t blo = 0;
+        uint32_t base = 0;  // start of the slab in the gene's bucket order (elements of earlier
+                            // slabs; kept here, since hall[blo] counts up during the scatter)
         for (uint32_t slab = 0; slab < nslabs; ++slab) {
-            if (tid == 0) {
-                uint32_t bh = (uint32_t)NB;
-                if (slab + 1u < nslabs) {  // first b >= blo whose start is >= (slab + 1) * W
+            // the slab's bucket range; the last slab ends at NB. (The scan, and the previous
+            // slab's rank phase, end with a block barrier.)
+            uint32_t bhi = (uint32_t)NB;
+            if (slab + 1u < nslabs) {
+                if (tid == 0) {  // first b >= blo whose start is >= (slab + 1) * W
                     uint32_t lo = blo, hi = (uint32_t)NB;
                     const uint32_t t1 = (slab + 1u) * W;
                     while (lo < hi) {
                         const uint32_t mid = (lo + hi) >> 1;
                         if (hall[mid] < t1) lo = mid + 1u; else hi = mid;
                     }
-                    bh = lo;
+                    s_slab_hi = lo;
                 }
-                s_slab_hi = bh;
+                __syncthreads();
+                bhi = s_slab_hi;
             }
-            __syncthreads();
-            const uint32_t bhi = s_slab_hi;
-            const uint32_t base = hall[blo], cnt_slab = hall[bhi] - base;
+            const uint32_t cnt_slab = hall[bhi] - base;  // hall[bhi] is outside this slab
             const bool in_smem = cnt_slab <= cap;
 
             // ---- pass 2 (L2): scatter this slab's decoded elements into bucket order ----
@@ -1037,9 +1042,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
                                        &s_pvq, a.erfc_table);
-            __syncthreads();
-            if (tid == 0) { s_chunk = 0u; s_nbig = 0u; s_bigi = 0u; s_wdone = 0u; }
             blo = bhi;
+            base += cnt_slab;
         }
         // pending p-values not taken in the rank phase (a gene without stored elements has none)
         if (pv_tk) pvalue_tiles(pv_tk, pv_c, &s_pvq, a.erfc_table);
