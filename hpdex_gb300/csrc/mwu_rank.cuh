@@ -12,8 +12,9 @@
 // slice for every target: reference ranks come from one bucket index per gene.
 //
 // Per gene:
-//   pass 1  (HBM, evict-first loads) 4-wide vector loads of row ids and values, group id
-//           gathers, decode to (key, group) written at the entry's position in the CTA's
+//   pass 1  (HBM, evict-first loads) warp tiles of 128 entries, 4 per lane with neighbouring
+//           lanes on neighbouring entries: row ids and values, group id gathers, decode to
+//           (key, group) written at the entry's position in the CTA's
 //           scratch slice; value-bucket histograms of all stored elements and of reference
 //           elements (bucket = top bits of key - column minimum key, from the resident
 //           matrix's column key ranges); per-group stored counts (negatives for mix)
@@ -31,7 +32,9 @@
 //           warps drain one bucket at a time with per-warp group counters: one
 //           representative per (run of equal keys, target) adds s*(2*lref + c0) to A and
 //           (c0+s)^3-(c0+s)-(c0^3-c0) to B
-//   final   zero block, U1, tie sum per target (fused: P during the next gene's rank phase)
+//   final   zero block, U1, tie sum per target (fused: P during the next gene's rank phase);
+//           the gene clears the bucket-table entries it used, and one thread fetches the
+//           next gene and its column metadata
 //
 // Shared-memory accumulators use 32-bit atomics (a 64-bit value is updated as two halves
 // with an explicit carry): on sm_103a a 64-bit shared atomic add costs about five times a
