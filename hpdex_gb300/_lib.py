@@ -58,12 +58,20 @@ EXPORTS = {
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.POINTER(MwuOptions), ctypes.c_int32,
                                           ctypes.c_void_p, ctypes.c_void_p]),
+    "hpdex_mannwhitneyu_idx32": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                                ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                                ctypes.POINTER(MwuOptions), ctypes.c_int32,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "hpdex_group_mean": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_void_p]),
     "hpdex_matrix_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_matrix_create_idx32": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "hpdex_matrix_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -78,7 +78,11 @@ def mannwhitneyu(data, indices, indptr, group_id, n_targets, ref_sorted=False, t
     Returns (U1, P), each float64 of shape (n_targets, n_genes), read-only."""
     n_targets = _check_size("n_targets", n_targets)
     data = _as_data(data)
-    indices = _as_index(indices)
+    indices = np.asarray(indices)
+    # int32 row ids (scipy's index type) go to the device as they are: half the bytes to
+    # upload and no host cast; anything else is cast to int64 as the reference binding takes
+    idx32 = indices.dtype == np.int32
+    indices = np.ascontiguousarray(indices) if idx32 else _as_index(indices)
     indptr = _as_index(indptr)
     group_id = np.ascontiguousarray(np.asarray(group_id), dtype=np.int32)
     R, C, nnz = group_id.size, indptr.size - 1, data.size
@@ -91,10 +95,10 @@ def mannwhitneyu(data, indices, indptr, group_id, n_targets, ref_sorted=False, t
     U1 = _lib.result_array((max(n_targets, 0), C))
     P = _lib.result_array((max(n_targets, 0), C))
     t0 = time.perf_counter()
-    st = _lib.lib().hpdex_mannwhitneyu(_DTYPES[data.dtype], data.ctypes.data, indices.ctypes.data,
-                                       indptr.ctypes.data, R, C, nnz, group_id.ctypes.data,
-                                       n_targets, opt, int(threads), U1.ctypes.data,
-                                       P.ctypes.data)
+    entry = _lib.lib().hpdex_mannwhitneyu_idx32 if idx32 else _lib.lib().hpdex_mannwhitneyu
+    st = entry(_DTYPES[data.dtype], data.ctypes.data, indices.ctypes.data, indptr.ctypes.data, R, C,
+               nnz, group_id.ctypes.data, n_targets, opt, int(threads), U1.ctypes.data,
+               P.ctypes.data)
     _lib.check(st)
     if show_progress:
         print(f"[hpdex_gb300] mannwhitneyu: {C} genes x {n_targets} targets in "

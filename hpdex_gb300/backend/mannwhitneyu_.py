@@ -1,6 +1,7 @@
 """Python wrappers with the reference's signatures (AI4Cell/hpdex
 src/hpdex/backend/mannwhitneyu_.py:28-127): scipy CSR/CSC in, string options mapped to the
-binding's integers, indices/indptr cast to int64 and group_id to int32."""
+binding's integers, indptr cast to int64 (indices to int64 unless they are int32) and group_id
+to int32."""
 from __future__ import annotations
 
 from typing import Literal
@@ -28,7 +29,11 @@ def _sparse_parts(sparse_matrix, group_id):
         raise ValueError(f"group_id must be 1D with length {R} (rows of CSC / cols of CSR)")
     group_id = group_id.astype(np.int32, copy=False)
     data = sparse_matrix.data
-    indices = sparse_matrix.indices.astype(np.int64, copy=False)
+    # int32 row ids stay int32: the binding takes them as they are (the reference casts to
+    # int64 here; the results are the same)
+    indices = sparse_matrix.indices
+    if indices.dtype != np.int32:
+        indices = indices.astype(np.int64, copy=False)
     indptr = sparse_matrix.indptr.astype(np.int64, copy=False)
     layout = "csc" if isinstance(sparse_matrix, scipy.sparse.csc_matrix) else "csr"
     return data, indices, indptr, group_id, layout

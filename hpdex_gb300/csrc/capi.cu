@@ -437,7 +437,10 @@ int validate_csc(const int64_t* indptr, long long n_cols, long long nnz, long lo
     return HPDEX_OK;
 }
 
-int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, const int64_t* indptr) {
+// Row ids: int64 (`indices`, narrowed on the device, ids outside [0, n_rows) marked -1) or
+// int32 (`indices32`, copied as they are; every consumer skips ids outside [0, n_rows)).
+int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, const int32_t* indices32,
+                  const int64_t* indptr) {
     const size_t vs = dtype_size(m->dtype);
     TRY(m->data.alloc(std::max<size_t>(1, (size_t)m->nnz * vs)));
     TRY(m->rows.alloc(std::max<long long>(1, m->nnz)));
@@ -447,7 +450,9 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
                         cudaMemcpyHostToDevice));
     // row ids: int64 -> int32 through a bounded staging buffer
     const long long chunk = 1ll << 24;
-    if (m->nnz) {
+    if (m->nnz && indices32) {
+        CUDA_TRY(cudaMemcpy(m->rows.p, indices32, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyHostToDevice));
+    } else if (m->nnz) {
         DevBuf<long long> stage;
         TRY(stage.alloc((size_t)std::min(chunk, m->nnz)));
         for (long long off = 0; off < m->nnz; off += chunk) {
@@ -863,9 +868,10 @@ struct TransposeLaunch {
     }
 };
 
-int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
-                      int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
-                      int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out);
+int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int32_t* indices32,
+                      const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                      const int32_t* group_id, int64_t n_targets, const hpdex_mwu_options* opt,
+                      double* U1_out, double* P_out);
 int matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
                       int32_t include_zeros, double* out);
 int plan_create(hpdex_matrix* m, const int32_t* group_id, int64_t n_targets,
@@ -1037,13 +1043,13 @@ int hpdex_device_sm_count(int32_t* sms) {
     return HPDEX_OK;
 }
 
-int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
-                        const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
-                        hpdex_matrix** out) {
+namespace {
+int matrix_create(int32_t dtype, const void* data, const int64_t* indices, const int32_t* indices32,
+                  const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz, hpdex_matrix** out) {
     if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
     *out = nullptr;
     if (dtype_size(dtype) == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
-    if (!indptr || (nnz > 0 && (!data || !indices))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    if (!indptr || (nnz > 0 && (!data || (!indices && !indices32)))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
     TRY(validate_csc(indptr, n_cols, nnz, n_rows));
     hpdex_matrix* m = new hpdex_matrix();
     m->dtype = dtype;
@@ -1051,10 +1057,23 @@ int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
     m->n_cols = n_cols;
     m->nnz = nnz;
     int st = device_info(m->dev);
-    if (st == HPDEX_OK) st = upload_matrix(m, data, indices, indptr);
+    if (st == HPDEX_OK) st = upload_matrix(m, data, indices, indices32, indptr);
     if (st != HPDEX_OK) { delete m; return st; }
     *out = m;
     return HPDEX_OK;
+}
+}  // namespace
+
+int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
+                        const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                        hpdex_matrix** out) {
+    return matrix_create(dtype, data, indices, nullptr, indptr, n_rows, n_cols, nnz, out);
+}
+
+int hpdex_matrix_create_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                              const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                              hpdex_matrix** out) {
+    return matrix_create(dtype, data, nullptr, indices, indptr, n_rows, n_cols, nnz, out);
 }
 
 int hpdex_matrix_destroy(hpdex_matrix* m) {
@@ -1259,8 +1278,8 @@ int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
     if (!opt) return fail(HPDEX_ERR_ARGUMENT, "options are NULL");
     if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
     if (opt->method != HPDEX_EXACT)
-        return oneshot_pipelined(dtype, data, indices, indptr, n_rows, n_cols, nnz, group_id, n_targets, opt,
-                                 U1_out, P_out);
+        return oneshot_pipelined(dtype, data, indices, nullptr, indptr, n_rows, n_cols, nnz, group_id, n_targets,
+                                 opt, U1_out, P_out);
     hpdex_matrix* m = nullptr;
     TRY(hpdex_matrix_create(dtype, data, indices, indptr, n_rows, n_cols, nnz, &m));
     hpdex_plan* p = nullptr;
@@ -1270,6 +1289,25 @@ int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
     hpdex_plan_destroy(p);
     hpdex_matrix_destroy(m);
     return st;
+}
+
+int hpdex_mannwhitneyu_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                             const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                             const int32_t* group_id, int64_t n_targets,
+                             const hpdex_mwu_options* opt, int32_t threads, double* U1_out,
+                             double* P_out) {
+    if (!opt) return fail(HPDEX_ERR_ARGUMENT, "options are NULL");
+    if (n_targets < 1) return fail(HPDEX_ERR_RUNTIME, "[mannwhitney] n_targets must be >= 1 (>=1 target groups)");
+    if (nnz < 0) return fail(HPDEX_ERR_ARGUMENT, "nnz must be >= 0");
+    if (opt->method != HPDEX_EXACT)
+        return oneshot_pipelined(dtype, data, nullptr, indices, indptr, n_rows, n_cols, nnz, group_id, n_targets,
+                                 opt, U1_out, P_out);
+    // exact p-values: through the int64 path
+    if (nnz > 0 && !indices) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    std::vector<int64_t> wide((size_t)nnz);
+    for (int64_t i = 0; i < nnz; ++i) wide[(size_t)i] = indices[i];
+    return hpdex_mannwhitneyu(dtype, data, wide.data(), indptr, n_rows, n_cols, nnz, group_id, n_targets, opt,
+                              threads, U1_out, P_out);
 }
 
 int hpdex_group_mean(int32_t dtype, const void* data, const int64_t* indices,
@@ -1396,12 +1434,17 @@ namespace {
 
 constexpr int kPipelineChunks = 12;
 
-int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int64_t* indptr,
-                      int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,
-                      int64_t n_targets, const hpdex_mwu_options* opt, double* U1_out, double* P_out) {
+// Row ids come as int64 (`indices`, narrowed on the device through staging buffers) or as
+// int32 (`indices32`, uploaded straight into the matrix: half the bytes; ids outside
+// [0, n_rows) are skipped by the rank kernel as the narrowing would mark them).
+int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, const int32_t* indices32,
+                      const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                      const int32_t* group_id, int64_t n_targets, const hpdex_mwu_options* opt,
+                      double* U1_out, double* P_out) {
     const size_t vs = dtype_size(dtype);
     if (vs == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
-    if (!indptr || (nnz > 0 && (!data || !indices))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
+    const bool idx32 = indices32 != nullptr;
+    if (!indptr || (nnz > 0 && (!data || (!indices && !indices32)))) return fail(HPDEX_ERR_ARGUMENT, "NULL matrix pointer");
     TRY(validate_csc(indptr, n_cols, nnz, n_rows));
     const long long C = n_cols;
 
@@ -1455,7 +1498,8 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     DevBuf<int32_t> queues;
     DevBuf<long long> stage[2];
     TRY(queues.alloc((size_t)K));
-    for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
+    if (!idx32)
+        for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
 
     struct Res {  // copy stream and events of this call, released once the copy stream drained
         cudaStream_t copy = nullptr;
@@ -1473,11 +1517,14 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     auto enqueue_copy = [&](int j) -> int {  // upload position j: chunk seq[j], staging buffer j & 1
         const int k = seq[(size_t)j];
         const long long p0 = indptr[cb[k]], nk = indptr[cb[k + 1]] - p0;
-        if (j >= 2) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (j - 2) + 1], 0));  // staging buffer free
+        if (j >= 2 && !idx32) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (j - 2) + 1], 0));  // staging buffer free
         if (nk) {
             CUDA_TRY(cudaMemcpyAsync(m->data.p + p0 * vs, static_cast<const unsigned char*>(data) + p0 * vs,
                                      (size_t)nk * vs, cudaMemcpyHostToDevice, sx));
-            CUDA_TRY(cudaMemcpyAsync(stage[j & 1].p, indices + p0, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, sx));
+            if (idx32)
+                CUDA_TRY(cudaMemcpyAsync(m->rows.p + p0, indices32 + p0, sizeof(int32_t) * nk, cudaMemcpyHostToDevice, sx));
+            else
+                CUDA_TRY(cudaMemcpyAsync(stage[j & 1].p, indices + p0, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, sx));
         }
         CUDA_TRY(cudaEventRecord(r.ev[2 * j], sx));
         return HPDEX_OK;
@@ -1567,7 +1614,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         const long long c0 = cb[k], c1 = cb[k + 1];
         const long long p0 = indptr[c0], nk = indptr[c1] - p0;
         CUDA_TRY(cudaStreamWaitEvent(sc, r.ev[2 * j], 0));
-        if (nk) {
+        if (nk && !idx32) {
             narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sc>>>(
                 stage[j & 1].p, m->rows.p + p0, nk, n_rows);
             CUDA_TRY(cudaGetLastError());

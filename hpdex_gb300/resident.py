@@ -40,17 +40,18 @@ class ResidentMatrix:
         data = np.ascontiguousarray(data)
         if data.dtype.name not in _lib.DTYPE_CODES:
             raise RuntimeError("Unsupported dtype for data")
-        indices = np.ascontiguousarray(indices, dtype=np.int64)
+        indices = np.asarray(indices)
+        idx32 = indices.dtype == np.int32  # int32 row ids are uploaded as they are
+        indices = np.ascontiguousarray(indices, dtype=np.int32 if idx32 else np.int64)
         indptr = np.ascontiguousarray(indptr, dtype=np.int64)
         self.n_rows = int(n_rows)
         self.n_cols = indptr.size - 1
         self.nnz = data.size
         self.dtype = data.dtype
         h = ctypes.c_void_p()
-        _lib.check(_lib.lib().hpdex_matrix_create(_lib.DTYPE_CODES[data.dtype.name],
-                                                  data.ctypes.data, indices.ctypes.data,
-                                                  indptr.ctypes.data, self.n_rows, self.n_cols,
-                                                  self.nnz, ctypes.byref(h)))
+        create = _lib.lib().hpdex_matrix_create_idx32 if idx32 else _lib.lib().hpdex_matrix_create
+        _lib.check(create(_lib.DTYPE_CODES[data.dtype.name], data.ctypes.data, indices.ctypes.data,
+                          indptr.ctypes.data, self.n_rows, self.n_cols, self.nnz, ctypes.byref(h)))
         self._h = h
 
     @classmethod

@@ -137,6 +137,14 @@ int hpdex_mannwhitneyu(int32_t dtype, const void* data, const int64_t* indices,
                        const hpdex_mwu_options* opt, int32_t threads, double* U1_out,
                        double* P_out);
 
+/* hpdex_mannwhitneyu with int32 row ids (scipy's index type below 2^31 entries): the same
+ * results, half the row-id bytes to upload, no cast to int64 on the host. */
+int hpdex_mannwhitneyu_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                             const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                             const int32_t* group_id, int64_t n_targets,
+                             const hpdex_mwu_options* opt, int32_t threads, double* U1_out,
+                             double* P_out);
+
 /* kernel.group_mean. out: n_cols * n_groups doubles, flat [gene * n_groups + g] exactly as
  * the reference. use_kahan is honoured as documented (the reference binding forwards
  * `threads` into it, module.cpp:211-213); both summation modes agree to ~1e-15 here. */
@@ -155,6 +163,11 @@ typedef struct hpdex_plan hpdex_plan;
 int hpdex_matrix_create(int32_t dtype, const void* data, const int64_t* indices,
                         const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
                         hpdex_matrix** out);
+/* hpdex_matrix_create with int32 row ids, copied as they are (ids outside [0, n_rows) are
+ * skipped by every kernel, as the int64 path's narrowing marks them). */
+int hpdex_matrix_create_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                              const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                              hpdex_matrix** out);
 /* The same resident matrix from a cells x genes CSR (AnnData's native layout; indptr over
  * the n_rows cells, indices = gene ids in [0, n_cols)), transposed on the device: columns hold
  * their rows in ascending order, entries with a gene id outside [0, n_cols) are dropped. */

@@ -1,6 +1,8 @@
 """GPU: the pipelined one-shot call (column chunks uploaded while earlier chunks are ranked,
 p-values written straight into the output arrays on coherent-memory systems) returns what the
 resident path returns, also after the device memory cache is released, and across dtypes."""
+import re
+
 import numpy as np
 import pytest
 
@@ -76,3 +78,46 @@ def test_results_in_pooled_page_locked_buffers():
     for U1, P in (b, c):
         np.testing.assert_array_equal(U1, ref[0])
         np.testing.assert_array_equal(P, ref[1])
+
+
+@pytest.mark.parametrize("zh", [0, 1, 3])
+def test_int32_row_ids_equal_int64(zh):
+    """Row ids given as int32 (uploaded as they are) give the int64 path's results, also with
+    row ids outside [0, n_rows), which both skip as the reference does."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.exact_small(seed=8, n_rows=3_000, n_cols=64, n_targets=40, ref_size=200)
+    w.data = np.round(w.data * 8) / 8
+    idx64 = w.indices.astype(np.int64).copy()
+    idx64[::97] = w.n_rows + 5
+    idx64[13::89] = -3
+    idx32 = idx64.astype(np.int32)
+    kw = dict(use_continuity=True, zero_handling=zh, fast_norm=False)
+    try:
+        r64 = kernel.mannwhitneyu(w.data, idx64, w.indptr, w.group_id, w.n_targets, **kw)
+    except RuntimeError as e:
+        with pytest.raises(RuntimeError, match=re.escape(str(e))):
+            kernel.mannwhitneyu(w.data, idx32, w.indptr, w.group_id, w.n_targets, **kw)
+        return
+    r32 = kernel.mannwhitneyu(w.data, idx32, w.indptr, w.group_id, w.n_targets, **kw)
+    np.testing.assert_array_equal(r32[0], r64[0])
+    np.testing.assert_array_equal(r32[1], r64[1])
+
+
+def test_int32_row_ids_resident_matrix():
+    """A resident matrix built from int32 row ids (with ids outside [0, n_rows)) gives the
+    int64-built matrix's results and group means."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix
+    w = synthetic.umi_counts(seed=5, n_rows=8_000, n_cols=120, n_targets=12)
+    idx64 = w.indices.astype(np.int64).copy()
+    idx64[::101] = w.n_rows + 7
+    idx64[7::103] = -1
+    out = []
+    for idx in (idx64, idx64.astype(np.int32)):
+        M = ResidentMatrix(w.data, idx, w.indptr, w.n_rows)
+        plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        plan.run()
+        out.append((*plan.download(), M.group_mean(w.group_id, w.n_targets + 1)))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)

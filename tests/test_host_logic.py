@@ -28,9 +28,15 @@ def test_option_maps_match_reference():
 
 def test_sparse_parts_casts_like_reference():
     X = sp.csc_matrix(np.eye(5, dtype=np.float64))
+    X.indices = X.indices.astype(np.int64)
     data, ind, ptr, gid, layout = W._sparse_parts(X, np.arange(5, dtype=np.int64))
     assert ind.dtype == np.int64 and ptr.dtype == np.int64 and gid.dtype == np.int32
     assert layout == "csc"
+    # int32 row ids (scipy's default) are passed on as int32, without a host cast
+    Y = sp.csc_matrix(np.eye(5, dtype=np.float64))
+    assert Y.indices.dtype == np.int32
+    _, ind32, ptr32, _, _ = W._sparse_parts(Y, np.arange(5))
+    assert ind32.dtype == np.int32 and ptr32.dtype == np.int64
 
 
 def test_de_group_selection():
