@@ -78,6 +78,9 @@ EXPORTS = {
     "hpdex_matrix_create_csr": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                                ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_matrix_create_csr_idx32": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                               ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "hpdex_matrix_group_mean": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                ctypes.c_int32, ctypes.c_void_p]),
     "hpdex_matrix_info": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int64)] * 4),

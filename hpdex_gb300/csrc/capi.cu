@@ -805,11 +805,13 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
 // Device transpose of a cells x genes CSR into the resident CSC layout (transpose.cuh).
 template <class V>
 struct TransposeLaunch {
-    static int run(hpdex_matrix* m, const void* h_data, const int64_t* h_genes, const int64_t* h_rowptr) {
+    template <class GI>  // gene ids: int64, or int32 (scipy's index type) uploaded as they are
+    static int run(hpdex_matrix* m, const void* h_data, const GI* h_genes, const int64_t* h_rowptr) {
         const long long R = m->n_rows, C = m->n_cols, nnz_in = m->nnz;
         const size_t vs = sizeof(V);
         DevBuf<unsigned char> dval;
-        DevBuf<int64_t> dgen, dptr, col_total;
+        DevBuf<GI> dgen;
+        DevBuf<int64_t> dptr, col_total;
         DevBuf<uint32_t> cnt;
         TRY(dval.alloc(std::max<size_t>(1, (size_t)nnz_in * vs)));
         TRY(dgen.alloc(std::max<long long>(1, nnz_in)));
@@ -817,7 +819,7 @@ struct TransposeLaunch {
         TRY(col_total.alloc(std::max<long long>(C, 1)));
         if (nnz_in) {
             CUDA_TRY(cudaMemcpy(dval.p, h_data, (size_t)nnz_in * vs, cudaMemcpyHostToDevice));
-            CUDA_TRY(cudaMemcpy(dgen.p, h_genes, sizeof(int64_t) * nnz_in, cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(dgen.p, h_genes, sizeof(GI) * nnz_in, cudaMemcpyHostToDevice));
         }
         CUDA_TRY(cudaMemcpy(dptr.p, h_rowptr, sizeof(int64_t) * (R + 1), cudaMemcpyHostToDevice));
         TRY(m->indptr.alloc((size_t)C + 1));
@@ -828,12 +830,12 @@ struct TransposeLaunch {
         const size_t smem = sizeof(uint32_t) * (size_t)C;
         const bool in_smem = smem <= 160 * 1024;
         if (in_smem) {
-            CUDA_TRY(cudaFuncSetAttribute(csr_block_count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            CUDA_TRY(cudaFuncSetAttribute(csr_scatter_kernel<V, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            csr_block_count_kernel<true><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
+            CUDA_TRY(cudaFuncSetAttribute(csr_block_count_kernel<true, GI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(csr_scatter_kernel<V, true, GI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            csr_block_count_kernel<true, GI><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
         } else {
             CUDA_TRY(cudaMemset(cnt.p, 0, sizeof(uint32_t) * (size_t)nb * C));
-            csr_block_count_kernel<false><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
+            csr_block_count_kernel<false, GI><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, R, rpb, (int)C, cnt.p);
         }
         CUDA_TRY(cudaGetLastError());
         if (C) {
@@ -849,11 +851,11 @@ struct TransposeLaunch {
         TRY(m->data.alloc(std::max<size_t>(1, (size_t)m->nnz * vs)));
         TRY(m->rows.alloc(std::max<long long>(1, m->nnz)));
         if (in_smem)
-            csr_scatter_kernel<V, true><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
+            csr_scatter_kernel<V, true, GI><<<nb, kTransposeThreads, smem>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
                                                                        (int)C, cnt.p, m->indptr.p, m->rows.p,
                                                                        reinterpret_cast<V*>(m->data.p));
         else
-            csr_scatter_kernel<V, false><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
+            csr_scatter_kernel<V, false, GI><<<nb, kTransposeThreads>>>(dptr.p, dgen.p, reinterpret_cast<const V*>(dval.p), R, rpb,
                                                                   (int)C, cnt.p, m->indptr.p, m->rows.p,
                                                                   reinterpret_cast<V*>(m->data.p));
         CUDA_TRY(cudaGetLastError());
@@ -1332,9 +1334,11 @@ int hpdex_matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int6
     return matrix_group_mean(m, group_id, n_groups, include_zeros, out);
 }
 
-int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indices,
-                            const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
-                            hpdex_matrix** out) {
+}  // extern "C"
+namespace {
+template <class GI>
+int matrix_create_csr(int32_t dtype, const void* data, const GI* indices, const int64_t* indptr,
+                      int64_t n_rows, int64_t n_cols, int64_t nnz, hpdex_matrix** out) {
     if (!out) return fail(HPDEX_ERR_ARGUMENT, "out is NULL");
     *out = nullptr;
     if (dtype_size(dtype) == 0) return fail(HPDEX_ERR_RUNTIME, "Unsupported dtype for data");
@@ -1362,6 +1366,20 @@ int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indi
     }
     *out = m.release();
     return HPDEX_OK;
+}
+}  // namespace
+extern "C" {
+
+int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indices,
+                            const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                            hpdex_matrix** out) {
+    return matrix_create_csr(dtype, data, indices, indptr, n_rows, n_cols, nnz, out);
+}
+
+int hpdex_matrix_create_csr_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                                  const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                  hpdex_matrix** out) {
+    return matrix_create_csr(dtype, data, indices, indptr, n_rows, n_cols, nnz, out);
 }
 
 }  // extern "C"

@@ -23,9 +23,9 @@ constexpr int kTransposeThreads = 256;
 
 // cnt[b * n_genes + c]: entries of rows [b*rpb, (b+1)*rpb) in column c. SMEM: a shared-memory
 // histogram (n_genes fits); else atomics straight into the block's row of cnt (zeroed first).
-template <bool SMEM>
+template <bool SMEM, class GI>  // GI: gene id type (int32 or int64)
 __global__ void __launch_bounds__(kTransposeThreads) csr_block_count_kernel(
-    const int64_t* indptr, const int64_t* genes, long long n_rows, long long rpb, int n_genes,
+    const int64_t* indptr, const GI* genes, long long n_rows, long long rpb, int n_genes,
     uint32_t* cnt) {
     extern __shared__ uint32_t hist_s[];
     uint32_t* out = cnt + (size_t)blockIdx.x * n_genes;
@@ -97,9 +97,9 @@ __global__ void __launch_bounds__(1024) column_pointer_scan_kernel(const int64_t
 }
 
 // SMEM: cursors in shared memory; else the block's row of offs serves as its cursors.
-template <class V, bool SMEM>
+template <class V, bool SMEM, class GI>
 __global__ void __launch_bounds__(kTransposeThreads) csr_scatter_kernel(
-    const int64_t* indptr, const int64_t* genes, const V* vals, long long n_rows, long long rpb,
+    const int64_t* indptr, const GI* genes, const V* vals, long long n_rows, long long rpb,
     int n_genes, uint32_t* offs, const int64_t* col_ptr, int32_t* rows_out, V* vals_out) {
     extern __shared__ uint32_t cursor_s[];
     uint32_t* o = offs + (size_t)blockIdx.x * n_genes;

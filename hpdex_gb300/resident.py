@@ -70,16 +70,18 @@ class ResidentMatrix:
         data = np.ascontiguousarray(data)
         if data.dtype.name not in _lib.DTYPE_CODES:
             raise RuntimeError("Unsupported dtype for data")
-        indices = np.ascontiguousarray(indices, dtype=np.int64)
+        indices = np.asarray(indices)
+        idx32 = indices.dtype == np.int32  # int32 gene ids are uploaded as they are
+        indices = np.ascontiguousarray(indices, dtype=np.int32 if idx32 else np.int64)
         indptr = np.ascontiguousarray(indptr, dtype=np.int64)
         self.n_rows, self.n_cols, self.dtype = int(n_rows), int(n_cols), data.dtype
         if indptr.size != self.n_rows + 1:
             raise ValueError("indptr must hold n_rows + 1 entries")
         h = ctypes.c_void_p()
-        _lib.check(_lib.lib().hpdex_matrix_create_csr(_lib.DTYPE_CODES[data.dtype.name],
-                                                      data.ctypes.data, indices.ctypes.data,
-                                                      indptr.ctypes.data, self.n_rows,
-                                                      self.n_cols, data.size, ctypes.byref(h)))
+        create = (_lib.lib().hpdex_matrix_create_csr_idx32 if idx32
+                  else _lib.lib().hpdex_matrix_create_csr)
+        _lib.check(create(_lib.DTYPE_CODES[data.dtype.name], data.ctypes.data, indices.ctypes.data,
+                          indptr.ctypes.data, self.n_rows, self.n_cols, data.size, ctypes.byref(h)))
         self._h = h
         self.nnz = self._info()[2]
         return self

@@ -174,6 +174,10 @@ int hpdex_matrix_create_idx32(int32_t dtype, const void* data, const int32_t* in
 int hpdex_matrix_create_csr(int32_t dtype, const void* data, const int64_t* indices,
                             const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
                             hpdex_matrix** out);
+/* hpdex_matrix_create_csr with int32 gene ids (scipy's index type), uploaded as they are. */
+int hpdex_matrix_create_csr_idx32(int32_t dtype, const void* data, const int32_t* indices,
+                                  const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                  hpdex_matrix** out);
 /* Per (gene, group) means of a resident matrix, flat [gene * n_groups + g]: the values of
  * hpdex_group_mean (reference group_mean_core, include_zeros as there). */
 int hpdex_matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,

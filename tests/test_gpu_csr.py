@@ -24,16 +24,20 @@ def _groups(n, rng, ref=300, T=6):
 def _compare(Xcsr, gid, T):
     from hpdex_gb300.resident import ResidentMatrix
     Xcsc = Xcsr.tocsc()
-    Mr = ResidentMatrix.from_scipy(Xcsr)
+    Mr = ResidentMatrix.from_scipy(Xcsr)  # int32 gene ids, uploaded as they are
+    Mr64 = ResidentMatrix.from_csr(Xcsr.data, Xcsr.indices.astype(np.int64), Xcsr.indptr,
+                                   *Xcsr.shape)
     Mc = ResidentMatrix(Xcsc.data, Xcsc.indices, Xcsc.indptr, Xcsc.shape[0])
-    assert Mr.nnz == Xcsc.nnz
+    Mc64 = ResidentMatrix(Xcsc.data, Xcsc.indices.astype(np.int64), Xcsc.indptr, Xcsc.shape[0])
+    assert Mr.nnz == Mr64.nnz == Xcsc.nnz
     out = []
-    for M in (Mr, Mc):
+    for M in (Mr, Mc, Mr64, Mc64):
         p = M.plan(gid, T, zero_handling="min", use_continuity=True)
         p.run()
         out.append(p.download() + (M.group_mean(gid, T + 1),))
-    for a, b in zip(out[0], out[1]):
-        np.testing.assert_array_equal(a, b)
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_csr_random_float():
@@ -67,15 +71,17 @@ def test_csr_out_of_range_gene_ids_are_dropped():
     good.sort_indices()
     gid, T = _groups(X.shape[0], rng, ref=150, T=3)
     Mr = ResidentMatrix.from_csr(X.data, indices, X.indptr, X.shape[0], X.shape[1])
+    Mr32 = ResidentMatrix.from_csr(X.data, indices.astype(np.int32), X.indptr, X.shape[0], X.shape[1])
     Mc = ResidentMatrix(good.data, good.indices, good.indptr, good.shape[0])
-    assert Mr.nnz == good.nnz
+    assert Mr.nnz == Mr32.nnz == good.nnz
     res = []
-    for M in (Mr, Mc):
+    for M in (Mr, Mc, Mr32):
         p = M.plan(gid, T, zero_handling="mix")
         p.run()
         res.append(p.download())
-    np.testing.assert_array_equal(res[0][0], res[1][0])
-    np.testing.assert_array_equal(res[0][1], res[1][1])
+    for other in res[1:]:
+        np.testing.assert_array_equal(res[0][0], other[0])
+        np.testing.assert_array_equal(res[0][1], other[1])
 
 
 def test_de_driver_csr_equals_csc():
