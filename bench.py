@@ -72,7 +72,7 @@ def peaks():
 
 def profile_figure(key):
     """A per-launch figure of the rank kernel from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "mwu_rank_kernel_perturb_screen.md")
+    path = os.path.join(ROOT, "profiles", "mwu_rank_kernel_perturb_screen.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
