@@ -421,7 +421,7 @@ def run_ours(args, rank, world):
         "gpu_launches": launches,
     }
     if rank == 0:
-        cpu_v, cores, sample = time_cpu(w, args.cpu_genes)
+        cpu_v, cores, sample = time_cpu(w, args.cpu_genes, reps=3)  # best of 3
         line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": sample}
         print(json.dumps(line), flush=True)
