@@ -30,7 +30,8 @@ def test_options_default_matches_reference_binding():
     from hpdex_gb300 import _lib
     o = _lib.MwuOptions()
     _lib.lib().hpdex_mwu_options_default(ctypes.byref(o))
-    # module.cpp:215-227 defaults (fast_norm is always the precise path here)
+    # module.cpp:215-227 defaults; the C default of fast_norm is 0 (the precise path), the
+    # Python binding passes the reference's fast_norm=True explicitly
     assert (o.ref_sorted, o.tar_sorted, o.tie_correction, o.use_continuity) == (0, 0, 1, 0)
     assert (o.zero_handling, o.alternative, o.method) == (0, 2, 2)
 
