@@ -90,8 +90,12 @@ int device_info(DeviceInfo& d) {
     CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)); d.smem_per_sm = (size_t)v;
     CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)); d.smem_optin = (size_t)v;
     CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev)); d.smem_reserved = (size_t)v;
-    // kernels may read and write pageable host memory directly (coherent host memory)
-    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev)); d.pageable_access = v != 0;
+    // kernels may read and write pageable host memory directly, through the host's page tables
+    // (coherent host memory, as on Grace); not where such access migrates pages on faults
+    int ats = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+    d.pageable_access = v != 0 && ats != 0;
     cache[dev] = d;
     return HPDEX_OK;
 }
@@ -143,6 +147,30 @@ __global__ void narrow_rows_kernel(const long long* in, int32_t* out, long long 
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const long long r = in[i];
         out[i] = (r >= 0 && r < n_rows) ? (int32_t)r : -1;
+    }
+}
+
+// Upload of one chunk read straight from the caller's host arrays (systems whose device reaches
+// pageable host memory): values copied, row ids narrowed to int32 (-1 outside [0, n_rows)).
+// kUploadCTAs CTAs of 1024 threads, four elements in flight per thread, keep the host link busy
+// from a few SMs while the persistent rank kernel of the previous chunk holds the others.
+constexpr int kUploadCTAs = 16;
+template <class V, class R>
+__global__ void __launch_bounds__(1024) upload_chunk_kernel(const V* __restrict__ hv, const R* __restrict__ hr,
+                                                            V* __restrict__ dv, int32_t* __restrict__ dr,
+                                                            long long n, long long n_rows) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    auto narrow = [&](R r) { return ((long long)r >= 0 && (long long)r < n_rows) ? (int32_t)r : -1; };
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const V v0 = hv[i], v1 = hv[i + stride], v2 = hv[i + 2 * stride], v3 = hv[i + 3 * stride];
+        const R r0 = hr[i], r1 = hr[i + stride], r2 = hr[i + 2 * stride], r3 = hr[i + 3 * stride];
+        dv[i] = v0; dv[i + stride] = v1; dv[i + 2 * stride] = v2; dv[i + 3 * stride] = v3;
+        dr[i] = narrow(r0); dr[i + stride] = narrow(r1); dr[i + 2 * stride] = narrow(r2); dr[i + 3 * stride] = narrow(r3);
+    }
+    for (; i < n; i += stride) {
+        dv[i] = hv[i];
+        dr[i] = narrow(hr[i]);
     }
 }
 
@@ -410,6 +438,22 @@ struct KeyRangeLaunch {
         const int grid = (int)std::max<long long>(1, std::min<long long>((entries + per_block - 1) / per_block, (long long)sms * 16));
         column_key_range_kernel<V><<<grid, 256, 0, s>>>(reinterpret_cast<const V*>(data), indptr, (int32_t)w,
                                                        kmin, kmax, hz);
+        CUDA_TRY(cudaGetLastError());
+        return HPDEX_OK;
+    }
+};
+
+template <class V>
+struct UploadLaunch {  // one chunk, straight from the host arrays (see upload_chunk_kernel)
+    static int run(const void* hv, const int64_t* hr64, const int32_t* hr32, void* dv, int32_t* dr,
+                   long long n, long long n_rows, cudaStream_t s) {
+        if (n == 0) return HPDEX_OK;
+        if (hr32)
+            upload_chunk_kernel<V, int32_t><<<kUploadCTAs, 1024, 0, s>>>(
+                static_cast<const V*>(hv), hr32, static_cast<V*>(dv), dr, n, n_rows);
+        else
+            upload_chunk_kernel<V, int64_t><<<kUploadCTAs, 1024, 0, s>>>(
+                static_cast<const V*>(hv), hr64, static_cast<V*>(dv), dr, n, n_rows);
         CUDA_TRY(cudaGetLastError());
         return HPDEX_OK;
     }
@@ -1516,7 +1560,11 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     DevBuf<int32_t> queues;
     DevBuf<long long> stage[2];
     TRY(queues.alloc((size_t)K));
-    if (!idx32)
+    // where the device reaches pageable host memory, a few CTAs read each chunk straight from the
+    // caller's arrays (no staging, no driver copies); else cudaMemcpyAsync (int64 row ids through
+    // staging buffers, narrowed on the device)
+    const bool kernel_upload = m->dev.pageable_access;
+    if (!idx32 && !kernel_upload)
         for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
 
     struct Res {  // copy stream and events of this call, released once the copy stream drained
@@ -1535,6 +1583,14 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     auto enqueue_copy = [&](int j) -> int {  // upload position j: chunk seq[j], staging buffer j & 1
         const int k = seq[(size_t)j];
         const long long p0 = indptr[cb[k]], nk = indptr[cb[k + 1]] - p0;
+        if (kernel_upload) {
+            TRY(dispatch_dtype<UploadLaunch>(dtype, static_cast<const void*>(static_cast<const unsigned char*>(data) + p0 * vs),
+                                             idx32 ? nullptr : indices + p0, idx32 ? indices32 + p0 : nullptr,
+                                             static_cast<void*>(m->data.p + p0 * vs), m->rows.p + p0, nk,
+                                             (long long)n_rows, sx));
+            CUDA_TRY(cudaEventRecord(r.ev[2 * j], sx));
+            return HPDEX_OK;
+        }
         if (j >= 2 && !idx32) CUDA_TRY(cudaStreamWaitEvent(sx, r.ev[2 * (j - 2) + 1], 0));  // staging buffer free
         if (nk) {
             CUDA_TRY(cudaMemcpyAsync(m->data.p + p0 * vs, static_cast<const unsigned char*>(data) + p0 * vs,
@@ -1632,7 +1688,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         const long long c0 = cb[k], c1 = cb[k + 1];
         const long long p0 = indptr[c0], nk = indptr[c1] - p0;
         CUDA_TRY(cudaStreamWaitEvent(sc, r.ev[2 * j], 0));
-        if (nk && !idx32) {
+        if (nk && !idx32 && !kernel_upload) {
             narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sc>>>(
                 stage[j & 1].p, m->rows.p + p0, nk, n_rows);
             CUDA_TRY(cudaGetLastError());
@@ -1646,7 +1702,9 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         ra.n_order = (int32_t)(c1 - c0);
         ra.queue = queues.p + k;
         ra.single_gene = -1;
-        TRY(rank_status(rank_launch(dtype, ra, p->rank_grid, p->rank_smem, sc), "rank kernel launch"));
+        // with kernel uploads, kUploadCTAs SMs stay free for the next chunk's upload
+        const int grid = kernel_upload ? std::max(1, p->rank_grid - kUploadCTAs) : p->rank_grid;
+        TRY(rank_status(rank_launch(dtype, ra, grid, p->rank_smem, sc), "rank kernel launch"));
         PArgs pa{};
         pa.U1 = p->U1.p;
         pa.P = p->P.p;
