@@ -1,9 +1,11 @@
 // capi.cu -- host orchestration and C ABI of the GB300 MWU backend (see
-// include/hpdex_gb300.h). Resident matrices, plans (a grouping over a matrix), the batched
-// and plain launch forms, exact-mode tables, and the one-shot calls that mirror the
-// reference binding kernel.mannwhitneyu / kernel.group_mean (AI4Cell/hpdex
-// src/cpp/module.cpp:193-243). No CPU fallback: without a usable device every entry
-// point fails with HPDEX_ERR_CUDA.
+// include/hpdex_gb300.h). Resident matrices (CSC or CSR input, int64 or int32 indices),
+// plans (a grouping over a matrix) with the batched (CUDA graph, fused p-values) and plain
+// launch forms, exact-mode tables, the pipelined one-shot calls that mirror the reference
+// binding kernel.mannwhitneyu / kernel.group_mean (AI4Cell/hpdex src/cpp/module.cpp:193-243),
+// the serving loop, the no-allocation entry point, BH FDR / fold change, the device memory
+// cache and the page-locked result-buffer pool. No CPU fallback: without a usable device
+// every entry point fails with HPDEX_ERR_CUDA.
 #include <cuda_runtime.h>
 
 #include <algorithm>
