@@ -265,6 +265,20 @@ def run_ours(args, rank, world):
     w = make_workload(args, rank)
     T, C = w.n_targets, w.n_cols
     tests = T * C
+    if args.only_oneshot:  # profiling runs: the public call only (warm-up, then `steps` calls)
+        kw = dict(tie_correction=True, use_continuity=True, zero_handling=1, fast_norm=False)
+        for _ in range(max(1, args.warmup)):
+            kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T, **kw)
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, T, **kw)
+            ts.append(time.perf_counter() - t0)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "form": "one-shot public call",
+                              "value": tests / statistics.median(ts),
+                              "median_ms": statistics.median(ts) * 1e3}), flush=True)
+        return 0
     M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
     plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
     if args.only_batched and args.separate_pvalues:
@@ -443,6 +457,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched form only (no plain form, e2e or CPU legs); for ncu")
+    ap.add_argument("--only-oneshot", action="store_true",
+                    help="time the public one-shot call only (for ncu)")
     ap.add_argument("--separate-pvalues", action="store_true",
                     help="with --only-batched: p-values in a separate kernel (for ncu)")
     args = ap.parse_args()
