@@ -156,7 +156,7 @@ __global__ void narrow_rows_kernel(const long long* in, int32_t* out, long long 
 // pageable host memory): values copied, row ids narrowed to int32 (-1 outside [0, n_rows)).
 // kUploadCTAs CTAs of 1024 threads, four elements in flight per thread, keep the host link busy
 // from a few SMs while the persistent rank kernel of the previous chunk holds the others.
-constexpr int kUploadCTAs = 16;
+constexpr int kUploadCTAs = 24;
 template <class V, class R>
 __global__ void __launch_bounds__(1024) upload_chunk_kernel(const V* __restrict__ hv, const R* __restrict__ hr,
                                                             V* __restrict__ dv, int32_t* __restrict__ dr,
