@@ -14,6 +14,11 @@ by the GB300 library through its C ABI (include/hpdex_gb300.h). Differences, by 
     vectorised form nests the polynomial differently, so its fast values are not reproduced
     bit for bit. The wrapper hpdex_gb300.backend.mannwhitneyu defaults to fast_norm=False.
   * threads only affects host-side preparation.
+  * indices may be int32 (scipy's index type): they are passed to the device as they are,
+    without the cast to int64 that the reference's wrapper does; any other integer type is
+    cast to int64 as before. The results are the same.
+  * U1 and P live in page-locked buffers from the library's pool when one is available (the
+    device writes them directly); a buffer returns to the pool with its array.
 """
 from __future__ import annotations
 
@@ -74,7 +79,8 @@ def mannwhitneyu(data, indices, indptr, group_id, n_targets, ref_sorted=False, t
     """Mann-Whitney U per (gene, target) of a CSC matrix grouped by `group_id`.
 
     `exact_variant` (extension, method=1 only): 0 reproduces the reference's exact p-values,
-    1 uses the true MWU null distribution (scipy semantics).
+    1 uses the true MWU null distribution (scipy semantics). int32 `indices` are taken as they
+    are (extension).
     Returns (U1, P), each float64 of shape (n_targets, n_genes), read-only."""
     n_targets = _check_size("n_targets", n_targets)
     data = _as_data(data)
