@@ -32,6 +32,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -200,6 +201,21 @@ def time_cpu(w, max_genes, reps=1):
     return tests / best, oracle.max_threads(), f"{sel.size} of {w.n_cols} genes (every {w.n_cols // sel.size}th), all 500 targets, {tests} tests, best of {reps}"
 
 
+def host_cpu():
+    """The host CPU's model name as lscpu reports it (Arm hosts have no 'model name' line in
+    /proc/cpuinfo), with the logical CPU count."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() == "Model name":
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return f"{model or platform.machine()}, {os.cpu_count()} logical CPUs"
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -221,7 +237,7 @@ def run_reference(args, rank, world):
         "config": {"workload": "perturb_screen 200000 cells x 8000 genes x 500 targets, "
                                "log1p-CP10k float32, zero_handling=min", "sample": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "cpu": host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -437,7 +453,7 @@ def run_ours(args, rank, world):
     if rank == 0:
         cpu_v, cores, sample = time_cpu(w, args.cpu_genes, reps=3)  # best of 3
         line["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": sample}
+                                "sample": sample, "cpu": host_cpu()}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -58,3 +58,12 @@ def test_exact_small_is_dense_with_small_groups():
     assert np.sum(g == 0) == 40
     sizes = np.bincount(g[g > 0], minlength=w.n_targets + 1)[1:]
     assert sizes.min() >= 3 and sizes.max() <= 40  # at most 38 distinct (n1, n2) pairs
+
+
+def test_umi_counts_low_location_variant_hits_the_nominal_density():
+    """With the mean's log-location at -3.5 instead of -1 the same NB model gives the nominal
+    ~7 % density."""
+    w = synthetic.umi_counts(n_cols=400, mu_log_loc=-3.5)
+    _valid_csc(w)
+    density = w.data.size / (w.n_rows * w.n_cols)
+    assert 0.05 < density < 0.09
