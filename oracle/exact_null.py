@@ -34,15 +34,26 @@ def mwu_counts(m: int, n: int) -> tuple:
     return tuple(poly)
 
 
+@lru_cache(maxsize=256)
+def mwu_tails(m: int, n: int) -> tuple:
+    """Integer tail sums sum_{v >= u} f(v) for u = 0..m*n."""
+    f = mwu_counts(m, n)
+    out = [0] * len(f)
+    s = 0
+    for u in range(len(f) - 1, -1, -1):
+        s += f[u]
+        out[u] = s
+    return tuple(out)
+
+
 def mwu_sf_exact(u: float, m: int, n: int) -> float:
     """P(U >= floor(u)) under the null, as the correctly rounded float64 of the fraction."""
     k = floor(u)
-    f = mwu_counts(m, n)
     if k <= 0:
         return 1.0
     if k > m * n:
         return 0.0
-    return float(Fraction(sum(f[k:]), comb(m + n, m)))
+    return float(Fraction(mwu_tails(m, n)[k], comb(m + n, m)))
 
 
 def p_exact(U1: float, m: int, n: int, alternative: int) -> float:

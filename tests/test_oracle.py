@@ -73,6 +73,24 @@ def test_oracle_exact_reference_discrepancy(oracle_lib):
     assert abs(2 * mwu_sf_exact(12, 5, 4) - 0.7301587301587301) < 1e-15
 
 
+def test_exact_null_matches_scipy_exact():
+    """The exact-integer MWU null (oracle/exact_null.py) against scipy's exact mode on tie-free
+    samples of the exact configuration's shapes (reference of up to 40, targets of 3-40):
+    x = reference, y = target, so scipy's statistic is U1."""
+    from scipy.stats import mannwhitneyu
+    from oracle.exact_null import p_exact
+    rng = np.random.default_rng(5)
+    names = {0: "less", 1: "greater", 2: "two-sided"}
+    for m, n in [(40, 3), (40, 17), (40, 40), (12, 30), (7, 5), (1, 9)]:
+        for _ in range(4):
+            z = rng.permutation(m + n).astype(np.float64)
+            x, y = z[:m], z[m:]
+            for alt, name in names.items():
+                r = mannwhitneyu(x, y, alternative=name, method="exact")
+                ours = p_exact(float(r.statistic), m, n, alt)
+                assert abs(ours - r.pvalue) <= 1e-12 * max(r.pvalue, 1e-300), (m, n, alt)
+
+
 def test_oracle_fast_norm_path_restates_reference_scalar_form():
     """fast_norm: Numerical Recipes erfcc (fractional error < 1.2e-7 of erfc), the reference's
     own arithmetic for mu and 1/sigma, and no clip of the two-sided p (|U1 - mu| < cc gives a
