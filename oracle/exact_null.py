@@ -1,6 +1,6 @@
 """Exact null distribution of the Mann-Whitney U statistic in Python integers.
 
-TEST INFRASTRUCTURE ONLY (checker for the GPU exact-mode tables).
+TEST INFRASTRUCTURE ONLY (oracle for the GPU exact-mode tables).
 
 The number of arrangements of m reference and n target observations (no ties) whose U
 equals u is the coefficient of q^u in the Gaussian binomial [m+n choose m]_q =

@@ -1,7 +1,7 @@
 /*
  * mwu_oracle.c -- CPU restatement of hpdex's Mann-Whitney U backend.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker for the GPU path and the
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle for the GPU path and the
  * "port" CPU baseline timed by bench.py. Only tests/, __graft_entry__.smoke() and
  * bench.py's CPU legs load it; the hpdex_gb300 product never links or calls it.
  *

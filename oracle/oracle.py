@@ -1,4 +1,4 @@
-"""ctypes front-end of the CPU checker (oracle/mwu_oracle.c).
+"""ctypes front-end of the CPU oracle (oracle/mwu_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
 legs. The hpdex_gb300 package never imports this module.
