@@ -229,9 +229,12 @@ def run_reference(args, rank, world):
         v, cores, sample = time_cpu(w, args.cpu_genes)
         vals.append(v)
     value = statistics.median(vals)
+    tests_per_step = cpu_sample(w, args.cpu_genes)[0].size * w.n_targets
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "steps": args.steps, "warmup": args.warmup,
+        # a step is one bounded sample of the workload (config.sample), timed on the host
+        "ms_per_step": tests_per_step / value * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": "perturb_screen 200000 cells x 8000 genes x 500 targets, "
