@@ -115,13 +115,20 @@ def random_query(rng, n_rows, ref_range=(1_000, 50_000), targets_range=(1, 200),
     T = int(np.floor(logu(targets_range[0], targets_range[1] + 1)))
     T = max(1, min(T, targets_range[1]))
     sizes = logu(*target_size_range, size=T).astype(np.int64)
+    if n_rows < 2 * (T + 1):
+        raise ValueError(f"{n_rows} cells cannot hold a reference and {T} targets of 2 cells")
     total = ref + int(sizes.sum())
     if total > n_rows:
         f = n_rows / total
         ref = max(2, int(ref * f))
         sizes = np.maximum(2, (sizes * f).astype(np.int64))
+        # every group keeps at least 2 cells (fewer make the query fail "Sample too small")
         while ref + sizes.sum() > n_rows:
-            sizes[np.argmax(sizes)] -= 1
+            k = int(np.argmax(sizes))
+            if sizes[k] > 2:
+                sizes[k] -= 1
+            else:
+                ref -= 1
     perm = rng.permutation(n_rows)
     gid = np.full(n_rows, -1, np.int32)
     gid[perm[:ref]] = 0
