@@ -9,7 +9,10 @@ header and hpdex_gb300/_lib.py must agree on every detail that is not checked at
 - hpdex_mwu_options has the layout of the ctypes structure: size and every field offset;
 - every declared function has the ctypes signature the header implies: return type, number
   of parameters, and per parameter the integer width and signedness, double or float, and for
-  pointers the pointee type wherever the binding names one.
+  pointers the pointee type wherever the binding names one;
+- the ctypes stub that INTEGRATION.md shows a maintainer of the reference runs against the
+  built library, binds hpdex_mannwhitneyu with the declared argument types and reports its
+  errors (no GPU is needed: the library refuses before it reads any array).
 """
 import ctypes
 import os
@@ -191,3 +194,35 @@ def test_signature_comparison_catches_a_planted_mismatch():
     assert _check_param("hpdex_matrix** out", ctypes.POINTER(ctypes.c_int64),
                         _lib.MwuOptions) is not None
     assert _check_param("const int64_t* indptr", ctypes.c_void_p, _lib.MwuOptions) is None
+
+
+def _integration_stub():
+    """The ctypes stub that INTEGRATION.md shows a maintainer of the reference."""
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        doc = f.read()
+    sec = doc[doc.index("## 3. The binding a reference maintainer would add"):]
+    return sec[sec.index("```python") + len("```python"):sec.index("```", sec.index("```python") + 9)]
+
+
+def test_integration_stub_binds_the_library_as_declared():
+    import numpy as np
+    from hpdex_gb300 import _lib
+    src = _integration_stub().replace('ctypes.CDLL("libhpdex_gb300.so")',
+                                      f"ctypes.CDLL({_lib.lib_path()!r})")
+    ns = {}
+    exec(compile(src, "INTEGRATION.md", "exec"), ns)
+    args = ns["lib"].hpdex_mannwhitneyu.argtypes
+    want = _lib.EXPORTS["hpdex_mannwhitneyu"][1]
+    assert len(args) == len(want)
+    for a, w in zip(args, want):
+        if isinstance(w, type) and issubclass(w, ctypes._Pointer):
+            assert issubclass(a, ctypes._Pointer) and a._type_._fields_ == w._type_._fields_
+        else:
+            assert a is w
+    with pytest.raises(RuntimeError, match="Unsupported dtype for data"):
+        ns["mannwhitneyu"](np.ones(4, np.float16), np.arange(4), np.array([0, 4]),
+                           np.zeros(4, np.int32), 1)
+    if _lib.device_count() == 0:
+        with pytest.raises(RuntimeError, match="no CUDA device"):
+            ns["mannwhitneyu"](np.ones(4, np.float32), np.arange(4), np.array([0, 4]),
+                               np.zeros(4, np.int32), 1)
