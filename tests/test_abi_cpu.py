@@ -226,3 +226,24 @@ def test_integration_stub_binds_the_library_as_declared():
         with pytest.raises(RuntimeError, match="no CUDA device"):
             ns["mannwhitneyu"](np.ones(4, np.float32), np.arange(4), np.array([0, 4]),
                                np.zeros(4, np.int32), 1)
+
+
+def test_integration_c_example_compiles_against_the_header(tmp_path):
+    """The C example of the integration notes, inside a function that declares its inputs,
+    compiles against the header with warnings as errors."""
+    cc = _compiler("gcc")
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
+        doc = f.read()
+    i = doc.index("```c\n") + len("```c\n")
+    body = doc[i:doc.index("```", i)]
+    body = "\n".join(ln for ln in body.splitlines() if not ln.startswith("#include"))
+    src = ("#include <stdio.h>\n#include <stdlib.h>\n#include \"hpdex_gb300.h\"\n"
+           "int run(const float* data, const int64_t* indices, const int64_t* indptr,\n"
+           "        int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,\n"
+           "        int64_t T, int64_t C) {\n" + body +
+           "\nfree(U1); free(P);\nreturn 0;\n}\n")
+    (tmp_path / "example.c").write_text(src)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                        os.path.dirname(HEADER), str(tmp_path / "example.c")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + src
