@@ -1,5 +1,5 @@
 // Stand-in for the reference's fast_norm p-value kernels (src/cpp/include/common.hpp),
-// which need Highway's vector exp. The checker build only supports fast_norm=False:
+// which need Highway's vector exp. The oracle build only supports fast_norm=False:
 // the fast entry points raise instead of returning numbers that were never pinned.
 #pragma once
 #include "macro.hpp"
@@ -10,14 +10,14 @@
 namespace hpdex {
 inline void array_p_asymptotic_two_sided(const double*, const double*, const double*,
                                          const double*, const double*, double*, size_t) {
-    throw std::runtime_error("fast_norm is unavailable in the checker build of the reference");
+    throw std::runtime_error("fast_norm is unavailable in the oracle build of the reference");
 }
 inline void array_p_asymptotic_greater(const double*, const double*, const double*,
                                        const double*, const double*, double*, size_t) {
-    throw std::runtime_error("fast_norm is unavailable in the checker build of the reference");
+    throw std::runtime_error("fast_norm is unavailable in the oracle build of the reference");
 }
 inline void array_p_asymptotic_less(const double*, const double*, const double*,
                                     const double*, const double*, double*, size_t) {
-    throw std::runtime_error("fast_norm is unavailable in the checker build of the reference");
+    throw std::runtime_error("fast_norm is unavailable in the oracle build of the reference");
 }
 }  // namespace hpdex

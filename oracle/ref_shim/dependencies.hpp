@@ -1,5 +1,5 @@
 // Stand-in for the reference's third-party include bundle, used only to build the
-// reference's own CPU kernel here as a checker. The reference pulls OpenMP and
+// reference's own CPU kernel here for the oracle tests. The reference pulls OpenMP and
 // Google Highway (an un-vendored, unpinned submodule that is empty in this checkout).
 // Only VQSortStatic(ptr, n, SortAscending()) is reached on the precise path
 // (src/cpp/mannwhitneyu.cpp:882); an exact std::sort gives the same sorted order,
