@@ -115,3 +115,20 @@ def test_oracle_equals_reference_kernel_on_random_cases(ref_kernel, oracle_lib, 
                 mo = oracle_lib.group_mean(data, indices, indptr, gid, T + 1, include_zeros, 2,
                                            kahan)
                 np.testing.assert_array_equal(mo, np.asarray(mr), err_msg=f"means {k}")
+
+
+@pytest.mark.parametrize("alt", [0, 1, 2])
+def test_oracle_exact_reference_variant_at_forty_reference_cells(ref_kernel, oracle_lib, alt):
+    """The exact configuration's shape: 40 reference cells and targets of 3-40 cells, where the
+    reference's uint64 composition count wraps. The oracle must wrap the same way."""
+    from hpdex_gb300 import synthetic
+    w = synthetic.exact_small(seed=23, n_rows=4_000, n_cols=5, n_targets=60, ref_size=40)
+    args = (w.data, w.indices, w.indptr, w.group_id, w.n_targets)
+    U1r, Pr = ref_kernel.mannwhitneyu(*args, False, False, True, False, False, 0, alt, 1, 1,
+                                      "csc", False)
+    U1o, Po = oracle_lib.mannwhitneyu(*args, tie_correction=True, use_continuity=False,
+                                      zero_handling=0, alternative=alt, method=1, threads=2)
+    np.testing.assert_array_equal(U1o, np.asarray(U1r))
+    np.testing.assert_array_equal(Po, np.asarray(Pr))
+    sizes = np.bincount(w.group_id[w.group_id >= 0], minlength=w.n_targets + 1)
+    assert sizes[0] == 40 and sizes[1:].max() >= 30
