@@ -132,3 +132,23 @@ def test_oracle_exact_reference_variant_at_forty_reference_cells(ref_kernel, ora
     np.testing.assert_array_equal(Po, np.asarray(Pr))
     sizes = np.bincount(w.group_id[w.group_id >= 0], minlength=w.n_targets + 1)
     assert sizes[0] == 40 and sizes[1:].max() >= 30
+
+
+@pytest.mark.parametrize("zh", [1, 2, 3])
+@pytest.mark.parametrize("workload", ["perturb_screen", "umi_counts"])
+def test_oracle_equals_reference_kernel_on_scaled_workloads(ref_kernel, oracle_lib, workload, zh):
+    """Scaled-down copies of the benchmark's screen and of the integer-count workload
+    (heavy ties), in the zero modes that place an implicit-zero block."""
+    from hpdex_gb300 import synthetic
+    if workload == "perturb_screen":
+        w = synthetic.perturb_screen(seed=101, n_rows=30_000, n_cols=300, n_targets=60,
+                                     ref_size=3_000)
+    else:
+        w = synthetic.umi_counts(seed=102, n_rows=20_000, n_cols=200, n_targets=20)
+    args = (w.data, w.indices.astype(np.int64), w.indptr, w.group_id, w.n_targets)
+    U1r, Pr = ref_kernel.mannwhitneyu(*args, False, False, True, True, False, zh, 2, 2, 1,
+                                      "csc", False)
+    U1o, Po = oracle_lib.mannwhitneyu(*args, tie_correction=True, use_continuity=True,
+                                      zero_handling=zh, alternative=2, method=2, threads=-1)
+    np.testing.assert_array_equal(U1o, np.asarray(U1r))
+    np.testing.assert_array_equal(Po, np.asarray(Pr))
