@@ -48,6 +48,7 @@ EXPORTS = {
     "hpdex_host_buffer_release": (ctypes.c_int, [ctypes.c_void_p]),
     "hpdex_selftest_erfc": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_selftest_erfc_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "hpdex_selftest_division": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64,
                                                ctypes.POINTER(ctypes.c_int64)]),
     "hpdex_bh_fdr": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
@@ -91,6 +92,7 @@ EXPORTS = {
     "hpdex_plan_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "hpdex_plan_set_fused_pvalues": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "hpdex_plan_set_drain_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                           ctypes.POINTER(ctypes.c_int32)]),
     "hpdex_mannwhitneyu_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,

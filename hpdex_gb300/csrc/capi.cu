@@ -963,6 +963,22 @@ int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_e
     return HPDEX_OK;
 }
 
+int hpdex_selftest_erfc_values(const double* x, int64_t n, double* out) {
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
+    DeviceInfo dev;
+    TRY(device_info(dev));
+    TRY(ensure_erfc_table());
+    if (n == 0) return HPDEX_OK;
+    DevBuf<double> buf;
+    TRY(buf.alloc(2 * (size_t)n));
+    CUDA_TRY(cudaMemcpy(buf.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)dev.sms * 8);
+    erfc_values_kernel<<<grid, 256>>>(buf.p, n, buf.p + n);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpy(out, buf.p + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    return HPDEX_OK;
+}
+
 int hpdex_selftest_division(int64_t n_cases, uint64_t seed, int64_t* mismatches) {
     if (n_cases < 0 || !mismatches) return fail(HPDEX_ERR_ARGUMENT, "bad arguments");
     DeviceInfo dev;
@@ -1296,6 +1312,16 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
     if (f == p->fused_pvalues) return HPDEX_OK;
     p->fused_pvalues = f;
     p->ra.erfc_table = f ? tbl : nullptr;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return HPDEX_OK;
+}
+
+int hpdex_plan_set_drain_wait(hpdex_plan* p, int32_t on) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    const int32_t off = on ? 0 : 1;
+    if (p->ra.no_drain_wait == off) return HPDEX_OK;
+    p->ra.no_drain_wait = off;
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
     if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
     return HPDEX_OK;
@@ -2372,19 +2398,28 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     // must start at zero (work counter, group sizes, longest column) and reset the error words
     CUDA_TRY(cudaMemsetAsync(base, 0, header_bytes, s));
     CUDA_TRY(cudaMemsetAsync(err, 0xff, kErrWords * sizeof(unsigned long long), s));
-    if (C == 0) return HPDEX_OK;
+    if (C == 0) {
+        CUDA_TRY(cudaStreamSynchronize(s));
+        return HPDEX_OK;
+    }
     {
         const int grid = (int)std::min<long long>(std::max<long long>((std::max<long long>((long long)n_rows, C) + 255) / 256, 1),
                                                   (long long)nd->info.sms * 4);
         noalloc_prepare_kernel<<<grid, 256, 0, s>>>(d_group_id, n_rows, G, d_indptr, (int)C, group_rows,
                                                     max_col, order);
-        CUDA_TRY(cudaGetLastError());
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) {
+            cudaStreamSynchronize(s);
+            return fail(HPDEX_ERR_CUDA, "no-alloc prepare kernel: %s", cudaGetErrorString(le));
+        }
     }
     long long rows_host[kNoAllocMaxGroups];
     unsigned long long longest = 0;
     CUDA_TRY(cudaMemcpyAsync(rows_host, group_rows, sizeof(long long) * G, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaMemcpyAsync(&longest, max_col, sizeof(longest), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
+    if (longest > 0 && (!d_data || !d_rows))
+        return fail(HPDEX_ERR_ARGUMENT, "NULL device pointer (values or row ids of a matrix with entries)");
     if (zh != HPDEX_ZERO_NONE) {  // same checks and messages as hpdex_plan_create
         if (rows_host[0] < 2) return fail(HPDEX_ERR_RUNTIME, "Sample too small for reference at column 0");
         for (int g = 1; g < G; ++g)
@@ -2415,7 +2450,11 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
         take(sizeof(uint32_t) * (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G)));
     // group of each row, 16-bit
     uint16_t* gidc = reinterpret_cast<uint16_t*>(take((size_t)std::max<long long>(n_rows, 1) * gb));
-    if (off > kNoAllocScratchBytes) return fail(HPDEX_ERR_UNSUPPORTED, "hpdex_mannwhitneyu_noalloc: scratch exhausted");
+    if (off > kNoAllocScratchBytes)
+        return fail(HPDEX_ERR_UNSUPPORTED,
+                    "hpdex_mannwhitneyu_noalloc: scratch exhausted: n_rows = %lld and n_targets = %lld "
+                    "need %zu of the %zu bytes before any column slice", (long long)n_rows,
+                    (long long)n_targets, off, kNoAllocScratchBytes);
     // per CTA: a decoded copy of the current column and, for columns larger than the
     // shared-memory capacity, a bucket-ordered slab slice
     const int nslices = (long long)longest > cap ? 2 : 1;
@@ -2430,6 +2469,9 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     void* dg = take((size_t)grid * slice * gb);
     void* ek = nslices == 2 ? take((size_t)grid * slice * kb) : nullptr;
     void* eg = nslices == 2 ? take((size_t)grid * slice * gb) : nullptr;
+    // from the first launch on, a failing step returns only after the stream has drained, so
+    // that a failed call leaves no work of its own running on the shared array
+    auto enqueue = [&]() -> int {
     {
         const int pg = (int)std::max<long long>(1, std::min<long long>((n_rows + 255) / 256, (long long)nd->info.sms * 8));
         prepare_group_ids_kernel<uint16_t><<<pg, 256, 0, s>>>(d_group_id, n_rows, G, gidc);
@@ -2496,6 +2538,12 @@ extern "C" int hpdex_mannwhitneyu_noalloc(int32_t dtype, const void* d_data, con
     pa.fast = opt->fast_norm;
     mwu_pvalue_asymptotic_kernel<<<(int)std::min<long long>((pa.n + 255) / 256, (long long)nd->info.sms * 8), 256, 0, s>>>(pa);
     CUDA_TRY(cudaGetLastError());
+    return HPDEX_OK;
+    };
+    if (const int rc = enqueue(); rc != HPDEX_OK) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
 
     unsigned long long e[kErrWords];
     CUDA_TRY(cudaMemcpyAsync(e, err, sizeof e, cudaMemcpyDeviceToHost, s));

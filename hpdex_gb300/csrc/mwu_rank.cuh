@@ -113,6 +113,8 @@ struct RankArgs {
     int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
     const double* erfc_table;  // non-null: the kernel also computes the asymptotic p-values
                                // (P replaces the tie sums); null: a p-value kernel follows
+    int32_t no_drain_wait;     // 1: a warp that finds a big-list entry not yet published gives
+                               // up at once (diagnostic: the results must not change)
 };
 
 constexpr int kMediumBucket = 32;  // 2..32: packed whole into warp rounds
@@ -578,7 +580,8 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
                           uint32_t* s_bigi, uint32_t* s_wdone, const Acc& acc, uint32_t* cnt,
                           uint32_t* wide_cnt, uint8_t* tbl, unsigned long long& tref,
-                          const RankTask* pv_tk, int pv_c, uint32_t* s_pvq, const double* erfc_table) {
+                          const RankTask* pv_tk, int pv_c, uint32_t* s_pvq, const double* erfc_table,
+                          int wait_polls) {
     const int lane = threadIdx.x & 31;
     const uint32_t nchunks = (bhi - blo + 31u) / 32u;
     // the previous gene's p-values (first slab only): kPvWarps warps, then they join the chunks
@@ -704,7 +707,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
                     if (q >= min(*(volatile uint32_t*)s_nbig, biglist_cap)) { st = 1; break; }
                     continue;
                 }
-                if (it >= kDrainWaitIters) { st = 2; break; }
+                if (it >= wait_polls) { st = 2; break; }
                 __nanosleep(64);
             }
         }
@@ -745,6 +748,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wait_polls = a.no_drain_wait ? 0 : kDrainWaitIters;
     const int GL = a.G;  // layout G
     const int NBMAX = 1 << a.nb_max_log2;
     const RankSmem L(a.nb_max_log2, GL, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,
@@ -1034,17 +1038,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 rank_slab<uint32_t, ACC_SMEM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
                                               biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                               wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
-                                              &s_pvq, a.erfc_table);
+                                              &s_pvq, a.erfc_table, wait_polls);
             else if (in_smem)
                 rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
-                                       &s_pvq, a.erfc_table);
+                                       &s_pvq, a.erfc_table, wait_polls);
             else
                 rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
-                                       &s_pvq, a.erfc_table);
+                                       &s_pvq, a.erfc_table, wait_polls);
             blo = bhi;
             base += cnt_slab;
         }

@@ -60,6 +60,13 @@ __global__ void erfc_check_kernel(long long n, unsigned long long* max_rel_bits,
     atomicMax(max_abs_bits, (unsigned long long)__double_as_longlong(ma));
 }
 
+// erfc_tab at given points (hpdex_selftest_erfc_values)
+__global__ void erfc_values_kernel(const double* x, long long n, double* out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = erfc_tab(x[i], g_erfc_table);
+}
+
 // Self-check of the divisions by a known reciprocal (pvalue_math.cuh) against IEEE division
 // (__ddiv_rn), bit for bit, on n generated cases; counts the mismatches. Case kinds (i % 4):
 //   0  tie sums by N (N - 1): integers below 2^53 over N in [2, 2^24]

@@ -140,6 +140,11 @@ class Plan:
         """Asymptotic p-values inside the rank kernel (default) or in a separate kernel."""
         _lib.check(_lib.lib().hpdex_plan_set_fused_pvalues(self._h, int(bool(on))))
 
+    def set_drain_wait(self, on: bool) -> None:
+        """Diagnostic: off makes the rank kernel's bounded waits for large buckets give up at
+        once, so the pass after the block barrier resolves them; results do not change."""
+        _lib.check(_lib.lib().hpdex_plan_set_drain_wait(self._h, int(bool(on))))
+
     def download(self):
         C = self.matrix.n_cols
         U1 = np.empty((self.n_targets, C), np.float64)

@@ -187,6 +187,50 @@ def exact_small(seed: int = 11, n_rows: int = 60_000, n_cols: int = 4_000, n_tar
                          method="exact"))
 
 
+def extreme_shift(seed: int = 31, n_cols: int = 400) -> Workload:
+    """Strong differential signal, for the deep tail of the p-values: 20,000 reference cells
+    and targets of 3,000, 1,000 and 3,000 cells (27,000 cells, all assigned). Values are
+    quantised sums of four uniform integers in [0, 63], / 16 (Irwin-Hall, sd ~2.3 units, so
+    ties occur); each target adds its own per-gene shift in sd units: target 1 U[0.6, 1.0]
+    (|z| near 30-48, around the p-values' subnormal range), target 2 U[1.2, 1.8], target 3
+    U[0, 1.6]. 70 % of the genes are dense, the rest keep each cell with probability U[0.5, 1)
+    (implicit zeros join the zero block). Only integer draws are used, so the arrays are
+    bit-identical on every platform and numpy version (the stored reference outputs depend on
+    that)."""
+    rng = np.random.default_rng(seed)
+    ref, sizes = 20_000, np.array([3_000, 1_000, 3_000])
+    n_rows = ref + int(sizes.sum())
+    gid = np.zeros(n_rows, np.int32)
+    pos = ref
+    for t, s in enumerate(sizes):
+        gid[pos:pos + s] = t + 1
+        pos += s
+    perm = rng.permutation(n_rows)  # integer-based shuffle
+    gid = gid[perm]
+    sd_units = 16.0 * np.sqrt(4 * (64 * 64 - 1) / 12.0) / 16.0  # sd of the integer sum, in 1/16
+    lo = np.array([0, 600, 1200, 0])  # shifts in thousandths of an sd, per target
+    hi = np.array([0, 1000, 1800, 1600])
+    rows_list, vals_list = [], []
+    indptr = np.zeros(n_cols + 1, np.int64)
+    for j in range(n_cols):
+        shift_milli = np.array([0] + [int(rng.integers(lo[t], hi[t] + 1)) for t in (1, 2, 3)])
+        # shift in 1/16 units, rounded to an integer so values stay exact in float32
+        shift16 = np.round(shift_milli * sd_units / 1000.0).astype(np.int64)
+        base = rng.integers(0, 64, size=(4, n_rows)).sum(axis=0)
+        v = base + shift16[gid]
+        if rng.integers(0, 10) < 7:
+            rows = np.arange(n_rows, dtype=np.int64)
+        else:
+            keep_milli = int(rng.integers(500, 1000))
+            rows = np.nonzero(rng.integers(0, 1000, size=n_rows) < keep_milli)[0].astype(np.int64)
+        rows_list.append(rows)
+        vals_list.append((v[rows] / 16.0).astype(np.float32))
+        indptr[j + 1] = indptr[j] + rows.size
+    return Workload("extreme_shift", n_rows, n_cols, np.concatenate(vals_list),
+                    np.concatenate(rows_list), indptr, gid, 3,
+                    dict(tie_correction=True, use_continuity=True, zero_handling="min"))
+
+
 WORKLOADS = {
     "small_float": small_float,
     "umi_counts": umi_counts,

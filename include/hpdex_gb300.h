@@ -121,6 +121,11 @@ int hpdex_fold_change(const double* means, int64_t n_genes, int64_t n_groups, do
  * 1e-300) and the largest absolute difference. */
 int hpdex_selftest_erfc(int64_t n_points, double* max_rel_err, double* max_abs_err);
 
+/* The p-value stage's erfc (table steps below 26.5, the deep-tail steps above) at n host
+ * points x, into host out: lets a test compare it with the host C library's erfc, which the
+ * reference calls (mannwhitneyu.cpp:21), including the subnormal tail. */
+int hpdex_selftest_erfc_values(const double* x, int64_t n, double* out);
+
 /* Self-check of the p-value stage's divisions by a precomputed reciprocal (Markstein's
  * correction steps) against IEEE division, bit for bit, on n_cases generated quotients (tie
  * sums over N (N - 1), random doubles, quotients next to a rounding midpoint, x / 12):
@@ -208,6 +213,13 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on);
 /* Copies U1 / P (n_targets x n_cols, target-major) to host; either pointer may be NULL. */
 int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
 
+/* Diagnostic. The rank kernel lets a warp resolve a large bucket while other warps of its CTA
+ * are still listing them; it waits a bounded number of polls for an entry to be published and,
+ * when they run out, leaves the entry to a pass after the next block barrier. on = 0 makes
+ * every such wait give up at once, so the fallback pass does all of that work; the results
+ * must not change (on = 1, the default, restores the bounded wait). */
+int hpdex_plan_set_drain_wait(hpdex_plan* p, int32_t on);
+
 /* Device times (ms, CUDA events on the launching stream) of the last hpdex_plan_run:
  * [0] whole run, [1] rank kernel(s) (with the p-values when fused), [2] p-value kernel
  * (0 when fused); and the number of kernel launches it made. */
@@ -232,9 +244,12 @@ int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches);
  * library; every GPU that loads the library holds it until the process exits. Limits:
  * n_targets + 1 <= HPDEX_NOALLOC_MAX_GROUPS, n_cols <= HPDEX_NOALLOC_MAX_COLS,
  * method = HPDEX_ASYMPTOTIC only, and the longest column must fit the per-SM element
- * slices that remain in the array (about 50k entries for float32 data); anything beyond
- * returns HPDEX_ERR_UNSUPPORTED with a message. Genes are taken in column order (no
- * longest-first scheduling).
+ * slices that remain in the array (about 50k entries for float32 data with few rows and
+ * targets). That column limit falls as n_rows and n_targets grow: the group ids take 2 bytes
+ * per row of the array and the per-warp run counters up to about 15 MB at 1,024 groups, so
+ * past roughly 30 million rows nothing is left. Anything beyond returns
+ * HPDEX_ERR_UNSUPPORTED with a message that gives the limit computed for the call. Genes are
+ * taken in column order (no longest-first scheduling).
  *
  * The first call on a device does a one-time set-up (it resolves the device address of
  * the array with cudaGetSymbolAddress); make that first call before any stream capture.

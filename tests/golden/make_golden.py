@@ -3,6 +3,7 @@
 Run in a checkout that has the reference sources (AI4Cell/hpdex) at /root/reference or
 $HPDEX_REFERENCE_ROOT:
     oracle/build_ref.sh && python tests/golden/make_golden.py
+(`python tests/golden/make_golden.py extreme_shift` writes the deep-tail fixture alone.)
 The reference module `kernel` (src/cpp/module.cpp) is built from its unmodified sources by
 oracle/build_ref.sh into oracle/_ref/. Every fixture stores its inputs next to the
 reference's outputs, so the tests never need the reference at run time.
@@ -105,7 +106,40 @@ def random_case(rng, R, C, T, dtype, dens, neg, ties, nonfinite, bad_rows=False,
     return data, indices, indptr, gid
 
 
+def input_digest(w):
+    """sha256 over the workload's arrays, stored beside its outputs so that a generator that
+    no longer reproduces the inputs fails loudly instead of comparing against stale outputs."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (w.data, w.indices.astype(np.int64), w.indptr.astype(np.int64),
+              w.group_id.astype(np.int32)):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def extreme_shift():
+    """Deep-tail fixture: the reference's U1 and P on synthetic.extreme_shift() (20,000
+    reference cells against targets of 3,000 / 1,000 / 3,000 cells, |z| up to ~90), for all
+    three alternatives with zero_handling='min' and both corrections on. Only the outputs and
+    an input digest are stored: the inputs regenerate from the seed (integer draws only)."""
+    w = synthetic.extreme_shift()
+    out = {}
+    for alt in (0, 1, 2):
+        o = dict(tie_correction=True, use_continuity=True, zero_handling=1, alternative=alt,
+                 method=2)
+        U1, P, err = run_ref(w.data, w.indices, w.indptr, w.group_id, w.n_targets, o)
+        assert not err, err
+        out[f"U1_alt{alt}"] = U1
+        out[f"P_alt{alt}"] = P
+    np.savez_compressed(os.path.join(HERE, "extreme_shift_outputs.npz"),
+                        digest=input_digest(w), n_targets=np.int64(w.n_targets), **out)
+    return "extreme_shift_outputs"
+
+
 def main():
+    if sys.argv[1:] == ["extreme_shift"]:
+        print("wrote", extreme_shift())
+        return
     written = []
     # 1) the CPU-runnable workload: 2,000 cells x 500 genes, 4 targets, min / tie / continuity
     w = synthetic.small_float()
@@ -188,6 +222,8 @@ def main():
                    method=1)
     save("exact_small_small", w.data, w.indices, w.indptr, w.group_id, w.n_targets, o_exact)
     written += ["umi_counts_small", "perturb_screen_small", "exact_small_small"]
+
+    extreme_shift()  # outputs only; not in the manifest of input+output fixtures
 
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
         json.dump(sorted(written), f, indent=0)

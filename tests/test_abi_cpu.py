@@ -10,9 +10,10 @@ header and hpdex_gb300/_lib.py must agree on every detail that is not checked at
 - every declared function has the ctypes signature the header implies: return type, number
   of parameters, and per parameter the integer width and signedness, double or float, and for
   pointers the pointee type wherever the binding names one;
-- the ctypes stub that INTEGRATION.md shows a maintainer of the reference runs against the
-  built library, binds hpdex_mannwhitneyu with the declared argument types and reports its
-  errors (no GPU is needed: the library refuses before it reads any array).
+- the ctypes stub a maintainer of the reference would add (hpdex_gb300/backend/bin/
+  ctypes_stub.py) runs against the built library, binds hpdex_mannwhitneyu with the declared
+  argument types and reports its errors (no GPU is needed: the library refuses before it reads
+  any array); the C example (include/hpdex_gb300_example.c) compiles against the header.
 """
 import ctypes
 import os
@@ -196,22 +197,12 @@ def test_signature_comparison_catches_a_planted_mismatch():
     assert _check_param("const int64_t* indptr", ctypes.c_void_p, _lib.MwuOptions) is None
 
 
-def _integration_stub():
-    """The ctypes stub that INTEGRATION.md shows a maintainer of the reference."""
-    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
-        doc = f.read()
-    sec = doc[doc.index("## 3. The binding a reference maintainer would add"):]
-    return sec[sec.index("```python") + len("```python"):sec.index("```", sec.index("```python") + 9)]
-
-
 def test_integration_stub_binds_the_library_as_declared():
     import numpy as np
     from hpdex_gb300 import _lib
-    src = _integration_stub().replace('ctypes.CDLL("libhpdex_gb300.so")',
-                                      f"ctypes.CDLL({_lib.lib_path()!r})")
-    ns = {}
-    exec(compile(src, "INTEGRATION.md", "exec"), ns)
-    args = ns["lib"].hpdex_mannwhitneyu.argtypes
+    from hpdex_gb300.backend.bin import ctypes_stub
+    lib, mannwhitneyu = ctypes_stub.bind(_lib.lib_path())
+    args = lib.hpdex_mannwhitneyu.argtypes
     want = _lib.EXPORTS["hpdex_mannwhitneyu"][1]
     assert len(args) == len(want)
     for a, w in zip(args, want):
@@ -220,30 +211,18 @@ def test_integration_stub_binds_the_library_as_declared():
         else:
             assert a is w
     with pytest.raises(RuntimeError, match="Unsupported dtype for data"):
-        ns["mannwhitneyu"](np.ones(4, np.float16), np.arange(4), np.array([0, 4]),
-                           np.zeros(4, np.int32), 1)
+        mannwhitneyu(np.ones(4, np.float16), np.arange(4), np.array([0, 4]),
+                     np.zeros(4, np.int32), 1)
     if _lib.device_count() == 0:
         with pytest.raises(RuntimeError, match="no CUDA device"):
-            ns["mannwhitneyu"](np.ones(4, np.float32), np.arange(4), np.array([0, 4]),
-                               np.zeros(4, np.int32), 1)
+            mannwhitneyu(np.ones(4, np.float32), np.arange(4), np.array([0, 4]),
+                         np.zeros(4, np.int32), 1)
 
 
-def test_integration_c_example_compiles_against_the_header(tmp_path):
-    """The C example of the integration notes, inside a function that declares its inputs,
-    compiles against the header with warnings as errors."""
+def test_c_example_compiles_against_the_header():
+    """include/hpdex_gb300_example.c compiles against the header as C99, warnings as errors."""
+    src = os.path.join(ROOT, "include", "hpdex_gb300_example.c")
     cc = _compiler("gcc")
-    with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
-        doc = f.read()
-    i = doc.index("```c\n") + len("```c\n")
-    body = doc[i:doc.index("```", i)]
-    body = "\n".join(ln for ln in body.splitlines() if not ln.startswith("#include"))
-    src = ("#include <stdio.h>\n#include <stdlib.h>\n#include \"hpdex_gb300.h\"\n"
-           "int run(const float* data, const int64_t* indices, const int64_t* indptr,\n"
-           "        int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* group_id,\n"
-           "        int64_t T, int64_t C) {\n" + body +
-           "\nfree(U1); free(P);\nreturn 0;\n}\n")
-    (tmp_path / "example.c").write_text(src)
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
-                        os.path.dirname(HEADER), str(tmp_path / "example.c")],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr + src
+                        os.path.dirname(HEADER), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

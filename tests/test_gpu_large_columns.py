@@ -90,3 +90,28 @@ def test_large_columns_many_targets():
     sizes = list(rng.integers(20, 400, size=300))
     w = _workload(4, 120_000, COLUMNS[:5], 20_000, sizes)
     assert _oracle_compare(w, zero_handling="min") == "ok"
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_drain_wait_fallback_gives_identical_results(fused):
+    """Warps that resolve listed big buckets while other warps still list them wait a bounded
+    number of polls for an entry; with no polls at all every such entry goes to the pass after
+    the block barrier. Both must give the same doubles, in both p-value forms."""
+    from hpdex_gb300.resident import BATCHED, ResidentMatrix
+    sizes = [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]
+    w = _workload(3, 150_000, COLUMNS, 30_000, sizes)
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    try:
+        plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        plan.set_fused_pvalues(fused)
+        plan.run(BATCHED)
+        U1a, Pa = plan.download()
+        plan.set_drain_wait(False)
+        for _ in range(2):
+            plan.run(BATCHED)
+            U1b, Pb = plan.download()
+            np.testing.assert_array_equal(U1b, U1a)
+            np.testing.assert_array_equal(Pb, Pa)
+        plan.close()
+    finally:
+        M.close()

@@ -153,3 +153,17 @@ def test_group_means_match_oracle(screen):
     m = kernel.group_mean(w.data, w.indices, w.indptr, w.group_id, G, include_zeros=True)
     mo = oracle.group_mean(w.data, w.indices, w.indptr, w.group_id, G, include_zeros=True)
     np.testing.assert_allclose(m, mo, rtol=1e-10, atol=0.0)
+
+
+def test_ranking_of_p_and_fdr_matches_oracle(screen, oracle_results, resident):
+    """All 4e6 tests ranked by P (stable argsort) in the same order as the oracle's P, and the
+    device's BH FDR of its own P ranking them as scipy's BH of the oracle's P does."""
+    from scipy.stats import false_discovery_control
+    from hpdex_gb300._lib import bh_fdr
+    w = screen
+    _, P = plan_results(resident, w, 1, 2)
+    _, Po = oracle_results(1, 2)
+    p, po = P.reshape(-1), np.ascontiguousarray(Po).reshape(-1)
+    np.testing.assert_array_equal(np.argsort(p, kind="stable"), np.argsort(po, kind="stable"))
+    fdr, fdr_o = bh_fdr(p), false_discovery_control(po, method="bh")
+    np.testing.assert_array_equal(np.argsort(fdr, kind="stable"), np.argsort(fdr_o, kind="stable"))
