@@ -16,7 +16,13 @@ One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
           group ids; D2H of U1 and P), wall clock. The call uploads the matrix in column
           chunks and ranks chunk k while chunk k+1 is in flight; on coherent-memory systems
           the p-value kernel writes U1 and P straight into the output arrays.
-  plain : the same call in the plain form (one launch per gene, no graph, no queue).
+  plain : the same plan in the plain form: one single-CTA launch per gene in column order, no
+          graph, no queue; the launches go round-robin to up to 128 concurrent streams, so the
+          comparison measures the queue and the graph, not idle SMs.
+  umi_counts: the 50,000 x 2,000 integer-count workload (49 targets): batched plan with the
+          per-gene histogram path against the bucket path only, group means, CPU port.
+  exact : the 60,000 x 4,000 dense exact-mode workload (40 reference cells, 1,500 targets):
+          both DP variants on the device, CPU port on a gene sample.
   serving: the serving loop (hpdex_gb300.serving) over three resident matrices (the
           200k x 8k screen, a 50k x 2k log1p-CP10k matrix and a 50k x 2k integer-count
           matrix), Poisson arrivals of random groupings (reference 1k-50k cells, 1-200
@@ -164,6 +170,77 @@ class ClockSampler:
                 "samples": len(use), "where": where}
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons through NVML's read-only queries, every `period` seconds
+    on a host thread, so that even a timed region of tens of milliseconds holds many samples.
+    stop() keeps the samples inside the timed region. Raises OSError when NVML is unavailable
+    (ClockSampler, over nvidia-smi, is the fallback)."""
+
+    # nvmlClocksEventReason bits (nvml.h)
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, gpu_index=0, period=0.002):
+        import ctypes
+        import threading
+        self.ct = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib = lib
+        self.h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu_index), ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML device")
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(self.h, ctypes.c_int(1), ctypes.byref(mx))  # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.rows = []
+        self.period = period
+        self.done = threading.Event()
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def _loop(self):
+        ct = self.ct
+        c, r = ct.c_uint(), ct.c_ulonglong()
+        while not self.done.is_set():
+            t = time.time()
+            if self.lib.nvmlDeviceGetClockInfo(self.h, ct.c_int(1), ct.byref(c)) == 0 and \
+                    self.reasons_fn(self.h, ct.byref(r)) == 0:
+                self.rows.append((t, float(c.value), int(r.value)))
+            time.sleep(self.period)
+
+    def wait_first(self, timeout=3.0):
+        t_end = time.time() + timeout
+        while not self.rows and time.time() < t_end:
+            time.sleep(0.001)
+
+    def stop(self, t_begin=None, t_end=None):
+        self.done.set()
+        self.t.join(timeout=2)
+        rows = self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["no samples"]}
+        inside = [x for x in rows if t_begin is None or t_begin <= x[0] <= t_end]
+        where = "inside the timed region"
+        if not inside:
+            mid = 0.5 * (t_begin + t_end)
+            inside, where = [min(rows, key=lambda x: abs(x[0] - mid))], "nearest to the timed region"
+        reasons = sorted({name for x in inside for bit, name in self.BITS.items() if x[2] & bit})
+        return {"sm_mhz": statistics.median(x[1] for x in inside), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(inside), "where": where,
+                "source": f"NVML every {self.period * 1e3:.0f} ms"}
+
+
+def clock_sampler():
+    try:
+        return NvmlSampler(0)
+    except (OSError, AttributeError):
+        return ClockSampler(0)
+
+
 def make_workload(args, rank):
     from hpdex_gb300 import synthetic
     return synthetic.perturb_screen(seed=7 + rank)
@@ -274,6 +351,122 @@ def serving_leg(M, w, queries=150, rates=(300.0, 1500.0)):
             "note": "latency = submit to results in host memory; tests/s over the run's wall time"}
 
 
+def time_plan(plan, steps, warmup=2):
+    """Device times (ms, CUDA events of the plan's stream) of `steps` batched runs."""
+    from hpdex_gb300.resident import BATCHED
+    for _ in range(warmup):
+        plan.run(BATCHED)
+    tot, rk = [], []
+    for _ in range(steps):
+        plan.run(BATCHED)
+        (t, r, _), _ = plan.timings()
+        tot.append(t)
+        rk.append(r)
+    return statistics.mean(tot), statistics.mean(rk)
+
+
+def time_cpu_workload(w, max_genes, reps, **opt):
+    """The oracle port (OpenMP, all host cores) on every k-th gene of w: tests/s, best of reps."""
+    from oracle import oracle
+    sel, data, ind, ip = cpu_sample(w, max_genes)
+    best = None
+    for _ in range(reps):
+        t = time.perf_counter()
+        oracle.mannwhitneyu(data, ind, ip, w.group_id, w.n_targets, threads=-1, **opt)
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    tests = sel.size * w.n_targets
+    return tests / best, oracle.max_threads(), \
+        f"{sel.size} of {w.n_cols} genes, all {w.n_targets} targets, {tests} tests, best of {reps}"
+
+
+def umi_leg(hbm, steps=20):
+    """Integer-count workload (50,000 cells x 2,000 genes, NB counts, 10,000 reference cells,
+    49 targets, zero_handling=min): the batched plan with the per-gene histogram path against the
+    same plan on the bucket path only; group means over G = 50; the oracle port on the host."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix
+    w = synthetic.umi_counts()
+    T, C = w.n_targets, w.n_cols
+    tests = T * C
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
+    hist_tot, hist_rank = time_plan(plan, steps)
+    U1h, Ph = plan.download()
+    plan.set_histogram(False)
+    buck_tot, buck_rank = time_plan(plan, steps)
+    U1b, Pb = plan.download()
+    plan.close()
+    gm = []
+    for _ in range(4):
+        t = time.perf_counter()
+        M.group_mean(w.group_id, T + 1, include_zeros=True)
+        gm.append(time.perf_counter() - t)
+    M.close()
+    B = algorithmic_bytes(w)
+    cpu_v, cores, sample = time_cpu_workload(w, C, 3, tie_correction=True, use_continuity=True,
+                                             zero_handling=1, alternative=2, method=2)
+    return {"workload": f"umi_counts: 50000 cells x 2000 genes, integral float32 NB counts "
+                        f"(realised density {w.nnz / (w.n_rows * C):.3f}, nnz={w.nnz}), 10000 "
+                        f"reference cells, {T} targets, zero_handling=min, tie+continuity",
+            "histogram": {"value": tests / (hist_tot / 1e3), "unit": UNIT, "ms_per_step": hist_tot,
+                          "rank_ms": hist_rank,
+                          "roofline": {"achieved": B / (hist_rank / 1e3) / 1e9, "peak": hbm,
+                                       "unit": "GB/s", "frac": B / (hist_rank / 1e3) / 1e9 / hbm,
+                                       "algorithmic_bytes": B}},
+            "bucket_only": {"value": tests / (buck_tot / 1e3), "unit": UNIT,
+                            "ms_per_step": buck_tot, "rank_ms": buck_rank},
+            "histogram_speedup": buck_tot / hist_tot,
+            "results_identical": bool(np.array_equal(U1h, U1b) and np.array_equal(Ph, Pb)),
+            "group_mean_ms": {"median": statistics.median(gm) * 1e3, "groups": T + 1,
+                              "note": "hpdex_matrix_group_mean, include_zeros, host wall incl. D2H"},
+            "steps": steps,
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample}}
+
+
+def exact_leg(steps=3):
+    """Exact-mode workload (60,000 cells x 4,000 genes dense float32 N(0,1) with per-target
+    shifts, 40 reference cells, 1,500 targets of 3-40 cells, zero_handling=none): device tests/s
+    for the reference-compatible DP variant and the true-null variant (rank kernel, then the
+    table build and lookup), and the oracle port on a gene sample on the host."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix
+    w = synthetic.exact_small()
+    T, C = w.n_targets, w.n_cols
+    tests = T * C
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    out = {"workload": "exact_small: 60000 cells x 4000 genes dense float32 (nnz 2.4e8), 40 "
+                       f"reference cells, {T} targets of 3-40 cells, zero_handling=none, "
+                       "method=exact, tie correction on, no continuity"}
+    for variant in ("reference", "mwu_null"):
+        plan = M.plan(w.group_id, T, zero_handling="none", use_continuity=False,
+                      tie_correction=True, method="exact", exact_variant=variant)
+        from hpdex_gb300.resident import BATCHED
+        plan.run(BATCHED)
+        tt, rk, tb = [], [], []
+        for _ in range(steps):
+            plan.run(BATCHED)
+            (t, r, p), _ = plan.timings()
+            tt.append(t)
+            rk.append(r)
+            tb.append(p)
+        plan.close()
+        out[variant] = {"value": tests / (statistics.median(tt) / 1e3), "unit": UNIT,
+                        "ms_per_step": statistics.median(tt), "rank_ms": statistics.median(rk),
+                        "tables_and_lookup_ms": statistics.median(tb)}
+    M.close()
+    cpu_v, cores, sample = time_cpu_workload(w, 200, 1, tie_correction=True, use_continuity=False,
+                                             zero_handling=0, alternative=2, method=1)
+    out["cpu_baseline"] = {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                           "variant": "reference (the reference's uint64 DP)", "sample": sample,
+                           "full_workload_s_estimate": tests / cpu_v}
+    out["reference_note"] = ("the reference's p_exact / p_exact_parallel "
+                             "(src/cpp/mannwhitneyu.cpp:98-188, :243-282); a survey-container "
+                             "estimate for the whole workload is about 15.3 s on 8 x86 cores")
+    return out
+
+
 def run_ours(args, rank, world):
     from hpdex_gb300 import _lib
     from hpdex_gb300.backend.bin import kernel
@@ -302,7 +495,7 @@ def run_ours(args, rank, world):
     plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
     if args.only_batched and args.separate_pvalues:
         plan.set_fused_pvalues(False)
-    sampler = ClockSampler(0)  # sampling from before the warm-up on
+    sampler = clock_sampler()  # sampling from before the warm-up on
     for _ in range(max(3, args.warmup)):
         plan.run(BATCHED)
     U1, P = plan.download()
@@ -388,8 +581,10 @@ def run_ours(args, rank, world):
     h2d32 = w.nnz * (w.data.itemsize + 4) + 8 * (C + 1) + 4 * w.n_rows
 
     serving = serving_leg(M, w) if not args.no_serving else None
-
     hbm, peak_kind = peaks()
+    umi = umi_leg(hbm) if not args.no_extra else None
+    exact = exact_leg() if not args.no_extra else None
+
     B = algorithmic_bytes(w)
     rank_avg = statistics.mean(rank_ms) / 1e3
     achieved = B / rank_avg / 1e9
@@ -428,6 +623,8 @@ def run_ours(args, rank, world):
                 "calls": e2e_steps, "mean_ms": e2e_wall * 1e3,
                 "value_from_mean": world * tests / e2e_wall,
                 "min_ms": min(e2e_calls) * 1e3, "max_ms": max(e2e_calls) * 1e3,
+                "note": f"median {statistics.median(e2e_calls) * 1e3:.2f} ms, mean "
+                        f"{e2e_wall * 1e3:.2f} ms over {e2e_steps} calls",
                 "call": "hpdex_gb300.backend.bin.kernel.mannwhitneyu (host numpy in/out, "
                         "fast_norm=False as the reference wrapper passes it)",
                 "int32_row_ids": {"value": world * tests / statistics.median(e2e32), "unit": UNIT,
@@ -445,6 +642,8 @@ def run_ours(args, rank, world):
                                          "total": min(x[0] for x in sep),
                                          "results_identical": same_sep}},
         "serving": serving,
+        "umi_counts": umi,
+        "exact": exact,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
                      "kernel": "mwu_rank_kernel", "algorithmic_bytes": B,
@@ -474,6 +673,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-genes", type=int, default=800)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the integer-count and exact-mode legs")
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched form only (no plain form, e2e or CPU legs); for ncu")
     ap.add_argument("--only-oneshot", action="store_true",

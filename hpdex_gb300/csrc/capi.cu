@@ -65,6 +65,8 @@ int fail(int code, const char* fmt, ...) {
     } while (0)
 
 constexpr int kRankThreads = 1024;
+constexpr int kPlainStreams = 128;  // concurrent streams of the plain form (the device runs at
+                                    // most 128 kernels at once)
 constexpr int kMeanThreads = 256;
 
 struct DeviceInfo {
@@ -394,7 +396,29 @@ struct hpdex_plan {
     cudaGraphExec_t graph_exec = nullptr;
     int last_launches = 0;
     float last_ms[3] = {0, 0, 0};
+    // plain form: concurrent streams for the per-gene launches, fork / join events
+    std::vector<cudaStream_t> plain_streams;
+    std::vector<cudaEvent_t> plain_join;
+    cudaEvent_t plain_fork = nullptr;
+    int ensure_plain_streams(int n) {
+        if (!plain_fork && cudaEventCreateWithFlags(&plain_fork, cudaEventDisableTiming) != cudaSuccess)
+            return fail(HPDEX_ERR_CUDA, "event create failed");
+        while ((int)plain_streams.size() < n) {
+            cudaStream_t st = nullptr;
+            cudaEvent_t ev = nullptr;
+            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+                return fail(HPDEX_ERR_CUDA, "stream create failed");
+            plain_streams.push_back(st);
+            if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+                return fail(HPDEX_ERR_CUDA, "event create failed");
+            plain_join.push_back(ev);
+        }
+        return HPDEX_OK;
+    }
     ~hpdex_plan() {
+        for (auto st : plain_streams) cudaStreamDestroy(st);
+        for (auto e : plain_join) cudaEventDestroy(e);
+        if (plain_fork) cudaEventDestroy(plain_fork);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
         for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -838,12 +862,29 @@ int enqueue_rank(hpdex_plan* p, int mode, cudaStream_t s, int* launches) {
         TRY(rank_status(rank_launch(p->m->dtype, p->ra, p->rank_grid, p->rank_smem, s), "rank kernel launch"));
         *launches += 1;
     } else {
-        for (long long c = 0; c < p->m->n_cols; ++c) {
+        // plain form: one single-CTA launch per gene, in column order, no queue and no graph;
+        // the launches go round-robin to concurrent streams (each on its own scratch slice) so
+        // that they fill the GPU as far as independent launches can
+        const int ns = std::max(1, std::min(p->rank_grid, kPlainStreams));
+        TRY(p->ensure_plain_streams(ns));
+        CUDA_TRY(cudaEventRecord(p->plain_fork, s));
+        for (int k = 0; k < ns; ++k) CUDA_TRY(cudaStreamWaitEvent(p->plain_streams[k], p->plain_fork, 0));
+        int st = HPDEX_OK;
+        for (long long c = 0; c < p->m->n_cols && st == HPDEX_OK; ++c) {
+            const int k = (int)(c % ns);
             p->ra.single_gene = (int32_t)c;
-            TRY(rank_status(rank_launch(p->m->dtype, p->ra, 1, p->rank_smem, s), "rank kernel launch"));
-            *launches += 1;
+            p->ra.cta_base = k;
+            st = rank_status(rank_launch(p->m->dtype, p->ra, 1, p->rank_smem, p->plain_streams[k]),
+                             "rank kernel launch");
+            if (st == HPDEX_OK) *launches += 1;
         }
         p->ra.single_gene = -1;
+        p->ra.cta_base = 0;
+        for (int k = 0; k < ns; ++k) {  // join (also after a failed launch)
+            CUDA_TRY(cudaEventRecord(p->plain_join[k], p->plain_streams[k]));
+            CUDA_TRY(cudaStreamWaitEvent(s, p->plain_join[k], 0));
+        }
+        TRY(st);
     }
     return HPDEX_OK;
 }
@@ -1312,6 +1353,16 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
     if (f == p->fused_pvalues) return HPDEX_OK;
     p->fused_pvalues = f;
     p->ra.erfc_table = f ? tbl : nullptr;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return HPDEX_OK;
+}
+
+int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    const int32_t off = on ? 0 : 1;
+    if (p->ra.no_histogram == off) return HPDEX_OK;
+    p->ra.no_histogram = off;
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
     if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
     return HPDEX_OK;

@@ -29,6 +29,17 @@ __device__ __forceinline__ unsigned long long key_of_f64(double v) {
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// inverses of the two float keys (the value of the double, -0.0 read back as +0.0)
+__device__ __forceinline__ float f32_of_key(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ double f64_of_key(unsigned long long k) {
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// Value traits: finite / zero / negative as the reference tests them, the order key, the
+// double the reference compares, small_int (an integer of magnitude below 2^31: such values
+// can be counted in integer bins) and the value back from a key.
 template <class V>
 struct Val;
 
@@ -43,6 +54,10 @@ struct Val;
             return (uint32_t)(int32_t)x ^ 0x80000000u;                                   \
         }                                                                                \
         static __device__ __forceinline__ double to_double(T x) { return (double)x; }   \
+        static __device__ __forceinline__ bool small_int(T) { return true; }             \
+        static __device__ __forceinline__ double from_key(Key k) {                       \
+            return (double)(int32_t)(k ^ 0x80000000u);                                   \
+        }                                                                                \
     };
 #define HPDEX_UNSIGNED_SMALL(T)                                                          \
     template <>                                                                          \
@@ -53,6 +68,8 @@ struct Val;
         static __device__ __forceinline__ bool neg(T) { return false; }                  \
         static __device__ __forceinline__ Key key(T x) { return (uint32_t)x; }           \
         static __device__ __forceinline__ double to_double(T x) { return (double)x; }   \
+        static __device__ __forceinline__ bool small_int(T x) { return x < 0x80000000u; } \
+        static __device__ __forceinline__ double from_key(Key k) { return (double)k; }   \
     };
 HPDEX_SIGNED_SMALL(int8_t)
 HPDEX_SIGNED_SMALL(int16_t)
@@ -73,6 +90,10 @@ struct Val<float> {
     static __device__ __forceinline__ bool neg(float x) { return x < 0.0f; }
     static __device__ __forceinline__ Key key(float x) { return key_of_f32(x); }
     static __device__ __forceinline__ double to_double(float x) { return (double)x; }
+    static __device__ __forceinline__ bool small_int(float x) {
+        return fabsf(x) < 2147483648.0f && x == truncf(x);
+    }
+    static __device__ __forceinline__ double from_key(Key k) { return (double)f32_of_key(k); }
 };
 template <>
 struct Val<double> {
@@ -84,6 +105,10 @@ struct Val<double> {
     static __device__ __forceinline__ bool neg(double x) { return x < 0.0; }
     static __device__ __forceinline__ Key key(double x) { return key_of_f64(x); }
     static __device__ __forceinline__ double to_double(double x) { return x; }
+    static __device__ __forceinline__ bool small_int(double x) {
+        return fabs(x) < 2147483648.0 && x == trunc(x);
+    }
+    static __device__ __forceinline__ double from_key(Key k) { return f64_of_key(k); }
 };
 template <>
 struct Val<int64_t> {
@@ -93,6 +118,10 @@ struct Val<int64_t> {
     static __device__ __forceinline__ bool neg(int64_t x) { return x < 0; }
     static __device__ __forceinline__ Key key(int64_t x) { return key_of_f64((double)x); }
     static __device__ __forceinline__ double to_double(int64_t x) { return (double)x; }
+    static __device__ __forceinline__ bool small_int(int64_t x) {
+        return x > -2147483648ll && x < 2147483648ll;
+    }
+    static __device__ __forceinline__ double from_key(Key k) { return f64_of_key(k); }
 };
 template <>
 struct Val<uint64_t> {
@@ -102,6 +131,8 @@ struct Val<uint64_t> {
     static __device__ __forceinline__ bool neg(uint64_t) { return false; }
     static __device__ __forceinline__ Key key(uint64_t x) { return key_of_f64((double)x); }
     static __device__ __forceinline__ double to_double(uint64_t x) { return (double)x; }
+    static __device__ __forceinline__ bool small_int(uint64_t x) { return x < 2147483648ull; }
+    static __device__ __forceinline__ double from_key(Key k) { return f64_of_key(k); }
 };
 
 __device__ __forceinline__ int bit_length(uint32_t x) { return 32 - __clz(x); }

@@ -65,7 +65,9 @@ struct RankTask {
     const int64_t* indptr;     // [n_cols + 1]
     const unsigned long long* col_kmin;  // per column min / max key of finite nonzero values
     const unsigned long long* col_kmax;  //   (kmin > kmax: none)
-    const uint32_t* col_has_zero;        // per column: stores an explicit finite zero
+    const uint32_t* col_has_zero;        // per column: bit 0 stores an explicit finite zero,
+                                         // bit 1 stores a finite value that is not an integer
+                                         // of magnitude below 2^31 (no histogram path)
     int64_t n_rows;
     int32_t n_cols;
     int32_t G;                 // n_targets + 1 (at most the launch's layout G)
@@ -115,6 +117,10 @@ struct RankArgs {
                                // (P replaces the tie sums); null: a p-value kernel follows
     int32_t no_drain_wait;     // 1: a warp that finds a big-list entry not yet published gives
                                // up at once (diagnostic: the results must not change)
+    int32_t no_histogram;      // 1: every gene takes the bucket path (the histogram path is
+                               // otherwise chosen per gene, see hist_choice)
+    int32_t cta_base;          // per-CTA scratch slice of CTA b: cta_base + b (the plain form
+                               // runs one-CTA launches on concurrent streams, each on its slice)
 };
 
 constexpr int kMediumBucket = 32;  // 2..32: packed whole into warp rounds
@@ -138,9 +144,10 @@ __host__ __device__ inline long long rank_slice(long long longest) {
     return ((longest > 0 ? longest : 1) + 63) & ~63ll;
 }
 
-// Shared-memory layout shared by host (sizing) and device (carving): bucket starts and
-// reference counts (NB + 1 each, padded to 16 bytes), the slab's list of large buckets, accumulators, run
-// counters, elements.
+// Shared-memory layout shared by host (sizing) and device (carving): accumulators, run
+// counters, then bucket starts and reference counts (NB + 1 each, padded to 16 bytes) with the
+// slab's list of large buckets, then elements. The last two are contiguous: a gene on the
+// histogram path uses both as its (value, group) counters.
 struct RankSmem {
     size_t hist_bytes, acc_bytes, cnt_bytes, elem_bytes, total;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -728,6 +735,142 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
     if (threadIdx.x == 0) { *s_chunk = 0u; *s_nbig = 0u; *s_bigi = 0u; *s_wdone = 0u; }
 }
 
+// ---------------------------------------------------------------------------------------
+// Histogram path, for genes whose stored values are small integers (UMI counts): one shared-
+// memory counter per (integer value, group), filled by one atomic per stored element in a
+// single streaming pass over the column (no decoded copy, no bucket scatter), then
+//     R[v]  = reference elements below value v    (exclusive block scan of row 0)
+//     r_v   = reference elements equal to v
+//     A[g]  = sum_v s_vg (2 R[v] + r_v),  B[g] = sum_v tie_delta(r_v, s_vg),  T_ref = sum_v r_v^3 - r_v
+// with s_vg the count of group g at v: the same integers the bucket path accumulates (the
+// reference's merge, mannwhitneyu.cpp:728-788), read off the counts, so the finalize is shared.
+// The counters of row g start at word 4 + g * Vp (row 0 at 0, with room for the scan's total).
+// A gene takes this path when its values are small integers (column flag), its value span V
+// is at most kHistMaxBins, and the V x G counters fit in the bucket-table + element region
+// and are not far more than its entries (hist_choice).
+// ---------------------------------------------------------------------------------------
+constexpr int kHistMaxBins = 8191;  // the block scan holds 8 entries per thread, V + 1 <= 8192
+
+__device__ __forceinline__ long long hist_words(int Vp, int G) {
+    return 4ll + (long long)G * Vp;
+}
+// Chooses the histogram path: span V of the integer values, the counters' words against the
+// region and against the gene's entries (each counter costs about a third of an entry).
+__device__ __forceinline__ bool hist_choice(long long lo, long long hi, int G, uint32_t nraw,
+                                            long long region_words, int* V, int* Vp) {
+    const long long span = hi - lo + 1;
+    if (span < 1 || span > kHistMaxBins) return false;
+    const int vp = (int)((span + 3) & ~3ll);
+    const long long w = hist_words(vp, G);
+    if (w > region_words || w > 3ll * nraw + 8192) return false;
+    *V = (int)span;
+    *Vp = vp;
+    return true;
+}
+
+// Exclusive prefix sum of x[0..L) in place, x[L] = total (L < 8 * NT; x 16-byte aligned).
+template <int NT>
+__device__ void block_scan1(uint32_t* x, int L, uint32_t* ws) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int beg = min(L, tid * 8), cnt = min(L, beg + 8) - beg;
+    uint32_t v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = i < cnt ? x[beg + i] : 0u;
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sum += v[i];
+    const uint32_t inc = warp_incl_scan(sum);
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    const uint32_t u = lane < NT / 32 ? ws[lane] : 0u;
+    const uint32_t pu = warp_incl_scan(u);
+    uint32_t o = __shfl_sync(0xffffffffu, pu - u, warp) + inc - sum;
+    if (warp == 0 && lane == 31) x[L] = pu;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (i < cnt) x[beg + i] = o;
+        o += v[i];
+    }
+    __syncthreads();
+}
+
+// One gene on the histogram path (hc: the counter region, 16-byte aligned); returns this
+// thread's share of T_ref. Not inlined, so that its registers stay out of the bucket path's
+// allocation. The caller's next block barrier orders its reads of the counters before the
+// region is cleared for the next gene.
+template <class V, int NT, class GT>
+static __device__ __noinline__ unsigned long long hist_gene(
+        uint32_t* hc, int hV, int hVp, long long hv0, int G, int zh, uint32_t nraw,
+        const int32_t* rows, const V* data, const GT* gidp, uint32_t nrows, Acc acc,
+        uint32_t* nz, uint32_t* ng, uint32_t* ws, const RankTask* pv_tk, int pv_c,
+        uint32_t* s_pvq, const double* erfc_table) {
+    constexpr uint32_t kNoGroup = (uint32_t)(GT)~GT(0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int words = (int)hist_words(hVp, G);
+    for (int i = 4 * tid; i < words; i += 4 * NT)
+        *reinterpret_cast<uint4*>(hc + i) = make_uint4(0u, 0u, 0u, 0u);
+    // the previous gene's p-values: as on the bucket path, some warps start on them
+    if (pv_tk && warp < kPvWarps) pvalue_tiles(pv_tk, pv_c, s_pvq, erfc_table);
+    __syncthreads();
+    // one streaming pass: each stored element increments its (value, group) counter
+    for (uint32_t i = (uint32_t)tid; i < nraw; i += 4u * NT) {
+        int32_t r[4];
+        V v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t e = i + (uint32_t)(k * NT);
+            r[k] = e < nraw ? __ldcs(rows + e) : -1;
+            v[k] = e < nraw ? ld_stream(data + e) : V(0);
+        }
+        uint32_t gl[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            gl[k] = (uint32_t)r[k] < nrows ? (uint32_t)__ldg(gidp + r[k]) : kNoGroup;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool ok = gl[k] != kNoGroup && Val<V>::finite(v[k]) &&
+                            (zh == ZH_NONE || !Val<V>::zero(v[k]));
+            if (ok) {
+                const uint32_t bin = (uint32_t)((long long)Val<V>::to_double(v[k]) - hv0);
+                red_add<true>(&hc[(gl[k] ? 4u + gl[k] * (uint32_t)hVp : 0u) + bin], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    block_scan1<NT>(hc, hV, ws);  // hc[v] = reference elements below v, hc[V] = all of them
+    // one warp per target group: its row against the reference's prefix counts
+    for (int g = 1 + warp; g < G; g += NT / 32) {
+        const uint32_t* row = hc + 4 + (size_t)g * hVp;
+        unsigned long long sa = 0, sb = 0;
+        uint32_t snz = 0, sng = 0;
+        for (int v = lane; v < hV; v += 32) {
+            const uint32_t sv = row[v];
+            if (sv) {
+                const uint32_t R = hc[v], rv = hc[v + 1] - R;
+                sa += (unsigned long long)sv * (2ull * R + rv);
+                sb += tie_delta(rv, sv);
+                snz += sv;
+                if (hv0 + v < 0) sng += sv;
+            }
+        }
+        sa = warp_sum_u64(sa);
+        sb = warp_sum_u64(sb);
+        snz = __reduce_add_sync(0xffffffffu, snz);
+        sng = __reduce_add_sync(0xffffffffu, sng);
+        if (lane == 0) { acc.A[g] = sa; acc.B[g] = sb; nz[g] = snz; ng[g] = sng; }
+    }
+    unsigned long long tref = 0ull;
+    for (int v = tid; v < hV; v += NT) {
+        const unsigned long long rv = hc[v + 1] - hc[v];
+        tref += rv * rv * rv - rv;
+    }
+    if (tid == 0) {
+        nz[0] = hc[hV];
+        ng[0] = hv0 < 0 ? hc[(int)min(-hv0, (long long)hV)] : 0u;
+    }
+    return tref;
+}
+
 template <class V, int NT, bool ACC_SMEM>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
@@ -755,19 +898,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                      (int)sizeof(K));
     const int cw = RankSmem::cnt_words(GL);
 
-    uint32_t* hall = reinterpret_cast<uint32_t*>(smem);  // bucket start (after the scan)
+    uint32_t* hall = reinterpret_cast<uint32_t*>(smem + L.acc_bytes + L.cnt_bytes);  // bucket
+                                                         // start (after the scan)
     uint32_t* href = hall + NBMAX + 4;                   // reference elements below a bucket
     uint32_t* biglist = href + NBMAX + 4;                // large buckets of the current slab
     const uint32_t biglist_cap = (uint32_t)RankSmem::big_list(
         RankSmem::compact_cap(a.elem_smem_cap, (int)sizeof(K), ACC_SMEM));
     unsigned char* accb;
     uint32_t* cnt_base;
-    uint32_t* cnt_glob = a.cnt_global + (size_t)blockIdx.x * a.tie_warps * (cw + GL);
+    const size_t cta = (size_t)a.cta_base + blockIdx.x;  // this CTA's scratch slices
+    uint32_t* cnt_glob = a.cnt_global + cta * a.tie_warps * (cw + GL);
     if constexpr (ACC_SMEM) {
-        accb = smem + L.hist_bytes;
-        cnt_base = reinterpret_cast<uint32_t*>(smem + L.hist_bytes + L.acc_bytes);
+        accb = smem;
+        cnt_base = reinterpret_cast<uint32_t*>(smem + L.acc_bytes);
     } else {
-        accb = a.acc_global + (size_t)blockIdx.x * 24 * GL;
+        accb = a.acc_global + cta * 24 * GL;
         cnt_base = cnt_glob;
     }
     unsigned long long* A = reinterpret_cast<unsigned long long*>(accb);
@@ -783,17 +928,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     // the element region holds a slab either with full keys (cap_full elements) or, when a
     // bucket spans at most 2^16 keys, with 16-bit offsets of the key inside its bucket
     // (cap_compact elements): within a bucket the offsets order like the keys
-    unsigned char* elem_base = smem + L.hist_bytes + L.acc_bytes + L.cnt_bytes;
+    unsigned char* elem_base = smem + L.acc_bytes + L.cnt_bytes + L.hist_bytes;
     const uint32_t cap_full = (uint32_t)a.elem_smem_cap;
     const uint32_t cap_compact = (uint32_t)RankSmem::compact_cap(a.elem_smem_cap, (int)sizeof(K), ACC_SMEM);
     K* ek_s = reinterpret_cast<K*>(elem_base);
     GT* eg_s = reinterpret_cast<GT*>(ek_s + cap_full);
     uint16_t* eo_s = reinterpret_cast<uint16_t*>(elem_base);
     GT* ego_s = reinterpret_cast<GT*>(eo_s + cap_compact);
-    K* dk = reinterpret_cast<K*>(a.dk_global) + (size_t)blockIdx.x * a.slice;
-    GT* dg = reinterpret_cast<GT*>(a.dg_global) + (size_t)blockIdx.x * a.slice;
-    K* ek_g = reinterpret_cast<K*>(a.ek_global) + (size_t)blockIdx.x * a.slice;
-    GT* eg_g = reinterpret_cast<GT*>(a.eg_global) + (size_t)blockIdx.x * a.slice;
+    K* dk = reinterpret_cast<K*>(a.dk_global) + cta * a.slice;
+    GT* dg = reinterpret_cast<GT*>(a.dg_global) + cta * a.slice;
+    K* ek_g = reinterpret_cast<K*>(a.ek_global) + cta * a.slice;
+    GT* eg_g = reinterpret_cast<GT*>(a.eg_global) + cta * a.slice;
 
     for (int i = tid; i < a.tie_warps * cw; i += NT) cnt_base[i] = 0u;
     for (int i = tid; i < a.tie_warps * GL; i += NT) wide_base[i] = 0u;
@@ -862,7 +1007,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
         // ---- bucket function from the column's key range ----
         K kmin = (K)s_next_kmin, kmax = (K)s_next_kmax;
-        if (zh == ZH_NONE && s_next_hz) {
+        if (zh == ZH_NONE && (s_next_hz & 1u)) {
             const K kz = Val<V>::key(V(0));
             kmin = kz < kmin ? kz : kmin;
             kmax = kz > kmax ? kz : kmax;
@@ -878,6 +1023,22 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         // (the bucket table is all zeros here: zeroed before the first gene, and each gene
         // clears the entries it used while it finalizes)
 
+        // ---- path: histogram (small integer values) or buckets ----
+        int hV = 0, hVp = 0;
+        long long hv0 = 0;
+        bool use_hist = false;
+        if constexpr (ACC_SMEM) {
+            if (!a.no_histogram && !(s_next_hz & 2u) && kmin <= kmax) {
+                hv0 = (long long)Val<V>::from_key(kmin);
+                use_hist = hist_choice(hv0, (long long)Val<V>::from_key(kmax), G, nraw,
+                                       (long long)((L.hist_bytes + L.elem_bytes) / 4), &hV, &hVp);
+            }
+        }
+        unsigned long long tref = 0ull;
+        if (use_hist) {
+            tref = hist_gene<V, NT, GT>(hall, hV, hVp, hv0, G, zh, nraw, rows, data, gidp, nrows,
+                                        acc, nz, ng, s_wsx, pv_tk, pv_c, &s_pvq, a.erfc_table);
+        } else {
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
         {
@@ -953,7 +1114,6 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         // During a slab's scatter hall[b] counts up from the start to the end of bucket b,
         // so afterwards the start of bucket b is hall[b - 1] (or the slab base for its first
         // bucket) and buckets of later slabs still hold their starts.
-        unsigned long long tref = 0ull;
         uint32_t blo = 0;
         uint32_t base = 0;  // start of the slab in the gene's bucket order (elements of earlier
                             // slabs; kept here, since hall[blo] counts up during the scatter)
@@ -1052,6 +1212,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             blo = bhi;
             base += cnt_slab;
         }
+        }  // bucket path
         // pending p-values not taken in the rank phase (a gene without stored elements has none)
         if (pv_tk) pvalue_tiles(pv_tk, pv_c, &s_pvq, a.erfc_table);
         tref = warp_sum_u64(tref);
@@ -1093,7 +1254,12 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             tk->U1[idx] = (double)u1x2 * 0.5;
             tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
         }
-        for (int b = tid; b <= NB; b += NT) { hall[b] = 0u; href[b] = 0u; }  // for the next gene
+        // for the next gene: a clear bucket table (all of it, and the big list, after the
+        // histogram path used the region for its counters)
+        const int nb_used = use_hist ? NBMAX : NB;
+        for (int b = tid; b <= nb_used; b += NT) { hall[b] = 0u; href[b] = 0u; }
+        if (use_hist)
+            for (uint32_t q = tid; q < biglist_cap; q += NT) biglist[q] = kInvalid;
         if (tid == 0 && a.erfc_table) {  // this gene's p-values: pending until the next gene
             s_pv_gene = c;
             s_pv_task = s_task;
@@ -1114,8 +1280,10 @@ __global__ void prepare_group_ids_kernel(const int32_t* gid, long long n_rows, i
     }
 }
 
-// Per-column key range of finite nonzero values and whether an explicit finite zero is
-// stored, for columns [0, n_cols) of `indptr` (entry positions into `data`). Entry-parallel:
+// Per-column key range of finite nonzero values, whether an explicit finite zero is stored
+// (bit 0 of has_zero) and whether a finite nonzero value is not a small integer (bit 1: the
+// column cannot take the histogram path), for columns [0, n_cols) of `indptr` (entry
+// positions into `data`). Entry-parallel:
 // a warp takes runs of 32 * kRangePer consecutive entries, lane l the kRangePer entries from
 // l * kRangePer; a lane folds the entries of one column at a time and publishes a column with
 // 64-bit atomics when it leaves it (a warp whose lanes all end in one column combines them
@@ -1137,14 +1305,14 @@ __global__ void column_key_range_kernel(const V* data, const int64_t* indptr, in
         const long long s1 = s0 + kRangePer < ee ? s0 + kRangePer : ee;
         int col = -1;
         K lo = ~K(0), hi = K(0);
-        bool z = false;
+        bool z = false, nonint = false;
         auto publish = [&](int c) {
             if (lo <= hi) {
                 atomicMin(&kmin[c], (unsigned long long)lo);
                 atomicMax(&kmax[c], (unsigned long long)hi);
             }
-            if (z) atomicOr(&has_zero[c], 1u);
-            lo = ~K(0); hi = K(0); z = false;
+            if (z || nonint) atomicOr(&has_zero[c], (z ? 1u : 0u) | (nonint ? 2u : 0u));
+            lo = ~K(0); hi = K(0); z = false; nonint = false;
         };
         if (s0 < ee) {
             int a = 0, b = n_cols - 1;  // the column holding s0: last c with indptr[c] <= s0
@@ -1159,6 +1327,7 @@ __global__ void column_key_range_kernel(const V* data, const int64_t* indptr, in
                 const V v = data[e];
                 if (!Val<V>::finite(v)) continue;
                 if (Val<V>::zero(v)) { z = true; continue; }
+                nonint |= !Val<V>::small_int(v);
                 const K k = Val<V>::key(v);
                 lo = k < lo ? k : lo;
                 hi = k > hi ? k : hi;
@@ -1169,6 +1338,7 @@ __global__ void column_key_range_kernel(const V* data, const int64_t* indptr, in
             lo = warp_min(lo);
             hi = warp_max(hi);
             z = __any_sync(0xffffffffu, z);
+            nonint = __any_sync(0xffffffffu, nonint);
             if (lane == 0 && c0 >= 0) publish(c0);
         } else if (col >= 0) {
             publish(col);

@@ -140,6 +140,11 @@ class Plan:
         """Asymptotic p-values inside the rank kernel (default) or in a separate kernel."""
         _lib.check(_lib.lib().hpdex_plan_set_fused_pvalues(self._h, int(bool(on))))
 
+    def set_histogram(self, on: bool) -> None:
+        """Per-gene histogram path for small-integer values (default) or the bucket path for
+        every gene; the results are the same."""
+        _lib.check(_lib.lib().hpdex_plan_set_histogram(self._h, int(bool(on))))
+
     def set_drain_wait(self, on: bool) -> None:
         """Diagnostic: off makes the rank kernel's bounded waits for large buckets give up at
         once, so the pass after the block barrier resolves them; results do not change."""

@@ -213,6 +213,13 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on);
 /* Copies U1 / P (n_targets x n_cols, target-major) to host; either pointer may be NULL. */
 int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
 
+/* The rank kernel takes each gene whose stored values are integers of magnitude below 2^31
+ * (UMI counts) and whose value span times the number of groups fits its shared memory through
+ * a histogram path: one counter per (value, group), rank sums from a prefix scan of the
+ * reference's counts. on = 0 sends every gene through the general (bucket) path instead, on = 1
+ * (the default) restores the per-gene choice. Both give the same results. */
+int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on);
+
 /* Diagnostic. The rank kernel lets a warp resolve a large bucket while other warps of its CTA
  * are still listing them; it waits a bounded number of polls for an entry to be published and,
  * when they run out, leaves the entry to a pass after the next block barrier. on = 0 makes
