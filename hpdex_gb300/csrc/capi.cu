@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -356,6 +357,8 @@ struct hpdex_matrix {
     DevBuf<uint32_t> col_has_zero;
     std::vector<long long> col_nnz;  // host copy for scheduling
     long long max_col_nnz = 0;
+    bool has_int_cols = true;  // some column stores only small integers (launches then use the
+                               // rank kernel with the histogram path)
     DeviceInfo dev;
 };
 
@@ -381,6 +384,7 @@ struct hpdex_plan {
     DevBuf<unsigned char> acc;
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
+    bool hist_on = true;         // histogram path allowed (hpdex_plan_set_histogram)
     bool fused_pvalues = false;  // asymptotic p-values computed inside the rank kernel
     size_t rank_smem = 0;
     int rank_grid = 0;
@@ -389,6 +393,8 @@ struct hpdex_plan {
     DevBuf<double> tables;
     DevBuf<unsigned long long> work;
     DevBuf<int32_t> pair_of_target, pair_of_test;
+    DevBuf<unsigned char> pair_mark;  // zero_handling none: (n1, n2) cells present
+    DevBuf<int32_t> pair_index;       //   and their pair ids
     // execution
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -495,6 +501,36 @@ struct MeanLaunch {
     }
 };
 
+// Sets m->has_int_cols from the column flags of the key-range pass: some column with finite
+// nonzero values, all of them small integers (bit 1 of col_has_zero clear).
+int matrix_int_hint(hpdex_matrix* m) {
+    const long long C = m->n_cols;
+    m->has_int_cols = false;
+    if (C == 0) return HPDEX_OK;
+    std::vector<uint32_t> f((size_t)C);
+    std::vector<unsigned long long> lo((size_t)C), hi((size_t)C);
+    CUDA_TRY(cudaMemcpy(f.data(), m->col_has_zero.p, sizeof(uint32_t) * C, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(lo.data(), m->col_kmin.p, sizeof(unsigned long long) * C, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(hi.data(), m->col_kmax.p, sizeof(unsigned long long) * C, cudaMemcpyDeviceToHost));
+    for (long long c = 0; c < C && !m->has_int_cols; ++c)
+        m->has_int_cols = !(f[(size_t)c] & 2u) && lo[(size_t)c] <= hi[(size_t)c];
+    return HPDEX_OK;
+}
+
+// The one-shot call's guess before any column is on the device: integer dtypes may hold small
+// integers; float data when its first (up to 4,096) values are finite integers. A wrong guess
+// only costs speed: both kernel variants give the same results.
+bool host_int_hint(int dtype, const void* data, long long nnz) {
+    if (dtype != HPDEX_FLOAT32 && dtype != HPDEX_FLOAT64) return true;
+    const long long n = std::min<long long>(nnz, 4096);
+    for (long long i = 0; i < n; ++i) {
+        const double v = dtype == HPDEX_FLOAT32 ? (double)static_cast<const float*>(data)[i]
+                                                : static_cast<const double*>(data)[i];
+        if (!(std::fabs(v) < 2147483648.0) || v != std::trunc(v)) return false;
+    }
+    return n > 0;
+}
+
 int validate_csc(const int64_t* indptr, long long n_cols, long long nnz, long long n_rows) {
     if (n_rows < 0 || n_cols < 0 || nnz < 0) return fail(HPDEX_ERR_ARGUMENT, "negative matrix size");
     if (n_rows >= (1ll << 31)) return fail(HPDEX_ERR_UNSUPPORTED, "n_rows must be below 2^31");
@@ -544,6 +580,7 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
                                            (cudaStream_t)0));
         CUDA_TRY(cudaDeviceSynchronize());
     }
+    TRY(matrix_int_hint(m));
     m->col_nnz.resize((size_t)m->n_cols);
     m->max_col_nnz = 0;
     for (long long c = 0; c < m->n_cols; ++c) {
@@ -682,6 +719,7 @@ int configure_rank(hpdex_plan* p) {
     a.n_order = (int32_t)m->n_cols;
     a.queue = p->queue.p;
     a.single_gene = -1;
+    a.no_histogram = (p->hist_on && m->has_int_cols) ? 0 : 1;
     set_layout_args(a, r, G, p->dk.p, p->dg.p, p->ek.p, p->eg.p, p->acc.p, p->cnt.p);
     return HPDEX_OK;
 }
@@ -715,7 +753,33 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
     if (n == 0) return HPDEX_OK;
     std::map<std::pair<long long, long long>, int> pairs;
     std::vector<int32_t> pot;  // pair of target / test
+    // zero_handling none, sizes in a small dense map: the device marks the (n1, n2) cells that
+    // occur and looks the pair of each test up in a dense index (no per-test host work)
+    long long H = 0, W = 0;
     if (p->opt.zero_handling == HPDEX_ZERO_NONE) {
+        H = p->group_rows[0] + 1;
+        for (long long t = 1; t <= T; ++t) W = std::max(W, p->group_rows[(size_t)t] + 1);
+    }
+    const bool dense_pairs = p->opt.zero_handling == HPDEX_ZERO_NONE && H * W <= (1ll << 22);
+    std::vector<int32_t> hidx;
+    if (dense_pairs) {
+        TRY(p->pair_mark.alloc((size_t)(H * W)));
+        CUDA_TRY(cudaMemsetAsync(p->pair_mark.p, 0, (size_t)(H * W), s));
+        const int g = (int)std::min<long long>((n + 255) / 256, (long long)p->m->dev.sms * 8);
+        exact_mark_pairs_kernel<<<g, 256, 0, s>>>(p->n1.p, p->n2.p, n, (int32_t)C, (int32_t)H,
+                                                  (int32_t)W, p->pair_mark.p);
+        CUDA_TRY(cudaGetLastError());
+        std::vector<unsigned char> mark((size_t)(H * W));
+        CUDA_TRY(cudaMemcpyAsync(mark.data(), p->pair_mark.p, mark.size(), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        hidx.assign((size_t)(H * W), -1);
+        for (long long r = 0; r < H * W; ++r)
+            if (mark[(size_t)r]) {
+                const int id = (int)pairs.size();
+                pairs.emplace(std::make_pair(r / W, r % W), id);
+                hidx[(size_t)r] = id;
+            }
+    } else if (p->opt.zero_handling == HPDEX_ZERO_NONE) {
         std::vector<uint32_t> h1((size_t)C), h2((size_t)n);
         CUDA_TRY(cudaStreamSynchronize(s));
         CUDA_TRY(cudaMemcpy(h1.data(), p->n1.p, sizeof(uint32_t) * C, cudaMemcpyDeviceToHost));
@@ -769,8 +833,15 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
     CUDA_TRY(cudaMemcpyAsync(p->pair_off.p, hoff.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(p->work_off.p, hwoff.data(), sizeof(long long) * np, cudaMemcpyHostToDevice, s));
     DevBuf<int32_t>& pmap = (p->opt.zero_handling == HPDEX_ZERO_NONE) ? p->pair_of_test : p->pair_of_target;
-    TRY(pmap.alloc(pot.size()));
-    CUDA_TRY(cudaMemcpyAsync(pmap.p, pot.data(), sizeof(int32_t) * pot.size(), cudaMemcpyHostToDevice, s));
+    if (!pot.empty()) {
+        TRY(pmap.alloc(pot.size()));
+        CUDA_TRY(cudaMemcpyAsync(pmap.p, pot.data(), sizeof(int32_t) * pot.size(), cudaMemcpyHostToDevice, s));
+    }
+    if (dense_pairs) {
+        TRY(p->pair_index.alloc(hidx.size()));
+        CUDA_TRY(cudaMemcpyAsync(p->pair_index.p, hidx.data(), sizeof(int32_t) * hidx.size(),
+                                 cudaMemcpyHostToDevice, s));
+    }
     ExactTables et{};
     et.pair_n1 = p->pair_n1.p;
     et.pair_n2 = p->pair_n2.p;
@@ -800,6 +871,9 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
     a.variant = p->opt.exact_variant;
     a.pair_of_target = p->pair_of_target.p;
     a.pair_of_test = p->pair_of_test.p;
+    a.pair_index = dense_pairs ? p->pair_index.p : nullptr;
+    a.pair_w = (int32_t)W;
+    a.pair_h = (int32_t)H;
     a.pair_n1 = p->pair_n1.p;
     a.pair_n2 = p->pair_n2.p;
     a.offset = p->pair_off.p;
@@ -1360,7 +1434,8 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
 
 int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on) {
     if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
-    const int32_t off = on ? 0 : 1;
+    p->hist_on = on != 0;
+    const int32_t off = (p->hist_on && p->m->has_int_cols) ? 0 : 1;
     if (p->ra.no_histogram == off) return HPDEX_OK;
     p->ra.no_histogram = off;
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
@@ -1487,6 +1562,7 @@ int matrix_create_csr(int32_t dtype, const void* data, const GI* indices, const 
                                            (cudaStream_t)0));
         CUDA_TRY(cudaDeviceSynchronize());
     }
+    TRY(matrix_int_hint(m.get()));
     *out = m.release();
     return HPDEX_OK;
 }
@@ -1607,6 +1683,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         m->col_nnz[(size_t)c] = indptr[c + 1] - indptr[c];
         m->max_col_nnz = std::max(m->max_col_nnz, m->col_nnz[(size_t)c]);
     }
+    m->has_int_cols = host_int_hint(dtype, data, nnz);
     if (C == 0) {
         CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t), cudaMemcpyHostToDevice));
         hpdex_plan* praw = nullptr;
@@ -2039,6 +2116,9 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         a.n_order = (int32_t)order.size();
         a.queue = b.queue.p;
         a.single_gene = -1;
+        bool any_int = false;  // the histogram variant when a query's matrix may hold integers
+        for (auto* q : b.q) any_int = any_int || S->mats[(size_t)q->matrix]->has_int_cols;
+        a.no_histogram = any_int ? 0 : 1;
         set_layout_args(a, r, GL, b.dk.p, b.dg.p, b.ek.p, b.eg.p, b.acc.p, b.cnt.p);
         TRY(rank_status(rank_launch(dtype, a, r.grid, r.smem, st), "rank kernel launch"));
     }

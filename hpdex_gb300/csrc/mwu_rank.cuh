@@ -117,8 +117,9 @@ struct RankArgs {
                                // (P replaces the tie sums); null: a p-value kernel follows
     int32_t no_drain_wait;     // 1: a warp that finds a big-list entry not yet published gives
                                // up at once (diagnostic: the results must not change)
-    int32_t no_histogram;      // 1: every gene takes the bucket path (the histogram path is
-                               // otherwise chosen per gene, see hist_choice)
+    int32_t no_histogram;      // 1: every gene takes the bucket path, and the launch uses the
+                               // kernel without the histogram path; 0: the histogram path is
+                               // chosen per gene (hist_choice)
     int32_t cta_base;          // per-CTA scratch slice of CTA b: cta_base + b (the plain form
                                // runs one-CTA launches on concurrent streams, each on its slice)
 };
@@ -736,6 +737,85 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
 }
 
 // ---------------------------------------------------------------------------------------
+// Bucket function of a gene. Buckets only need to be non-decreasing in the value (keys inside
+// a bucket are compared exactly), so the kernel picks, per gene:
+//   - (key - kmin) >> shift over the order keys. For floats the key bits are logarithmic in the
+//     value, which suits positive data (counts, log-expression) at any scale;
+//   - for a gene whose float values take both signs, (m(x) - m(xmin)) >> shift with
+//         m(x) = 2^(W-1) +- u(|x|),  u(t) = floor(t * 2^(M - E0))           for t <  2^E0
+//                                     u(t) = bits(t) - bits(2^E0) + 2^M    for t >= 2^E0
+//     (M mantissa bits, W key bits, 2^E0 = 2^-12 of min(|xmin|, |xmax|)): linear around zero,
+//     logarithmic beyond. Key bits alone would spend most buckets on the many binades of tiny
+//     magnitudes, leaving values near +-1 in a few large buckets of many distinct keys.
+// ---------------------------------------------------------------------------------------
+template <class V>
+struct BucketMap {
+    using K = typename Val<V>::Key;
+    static constexpr bool kFloat = std::is_same_v<V, float> || std::is_same_v<V, double>;
+    static constexpr int kKeyMap = -100000;  // e0 of the plain key map
+    K base = 0;                // kmin, or m(xmin)
+    int shift = 0;
+    int e0 = kKeyMap;          // E0 of the signed map (kKeyMap: the key map)
+    __device__ __forceinline__ bool vmap() const { return e0 != kKeyMap; }
+    __device__ __forceinline__ K m_of(K key) const {
+        if constexpr (std::is_same_v<V, float>) {
+            const float x = f32_of_key(key), t = fabsf(x);
+            const uint32_t bits = __float_as_uint(t), b0 = (uint32_t)(e0 + 127) << 23;
+            const uint32_t u = bits >= b0 ? bits - b0 + (1u << 23)
+                                          : (uint32_t)(t * __uint_as_float((uint32_t)(23 - e0 + 127) << 23));
+            return x < 0.0f ? 0x80000000u - u : 0x80000000u + u;
+        } else if constexpr (std::is_same_v<V, double>) {
+            const double x = f64_of_key(key), t = fabs(x);
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(t);
+            const unsigned long long b0 = (unsigned long long)(e0 + 1023) << 52;
+            const unsigned long long u = bits >= b0 ? bits - b0 + (1ull << 52)
+                : (unsigned long long)(t * __longlong_as_double((long long)(52 - e0 + 1023) << 52));
+            return x < 0.0 ? 0x8000000000000000ull - u : 0x8000000000000000ull + u;
+        } else {
+            return key;
+        }
+    }
+    // VM: the signed map (the caller picks it once per gene, outside its loops)
+    template <bool VM>
+    __device__ __forceinline__ uint32_t at(K key) const {
+        if constexpr (VM && kFloat) return (uint32_t)((m_of(key) - base) >> shift);
+        else return (uint32_t)((key - base) >> shift);
+    }
+    // whether a gene with key range [kmin, kmax] takes the signed map
+    static __device__ __forceinline__ bool signed_range(K kmin, K kmax) {
+        if constexpr (kFloat) {
+            const K k0 = Val<V>::key(V(0));
+            return kmin < k0 && kmax > k0;
+        } else {
+            return false;
+        }
+    }
+    // the bucket function of a gene with key range [kmin, kmax] and 2^nbl buckets
+    __device__ __forceinline__ void setup(K kmin, K kmax, int nbl) {
+        e0 = kKeyMap;
+        base = kmin;
+        K hi = kmax;
+        if constexpr (kFloat) {
+            if (signed_range(kmin, kmax)) {
+                // the smaller of the two extreme magnitudes: an outlier on one side does not
+                // stretch the linear part over the bulk of the values
+                const double amag = fmin(fabs(Val<V>::from_key(kmin)), fabs(Val<V>::from_key(kmax)));
+                const int ea = (int)(((unsigned long long)__double_as_longlong(amag) >> 52) & 0x7ff) - 1022;
+                // 2^E0 = 2^-12 of that magnitude, kept where 2^(M - E0) is a normal number
+                e0 = std::is_same_v<V, float> ? max(ea - 12, -100) : max(ea - 12, -960);
+                base = m_of(kmin);
+                hi = m_of(kmax);
+            }
+        }
+        shift = 0;
+        if (base <= hi) {
+            const int bl = bit_length(K(hi - base));
+            shift = bl > nbl ? bl - nbl : 0;
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------------------
 // Histogram path, for genes whose stored values are small integers (UMI counts): one shared-
 // memory counter per (integer value, group), filled by one atomic per stored element in a
 // single streaming pass over the column (no decoded copy, no bucket scatter), then
@@ -871,7 +951,9 @@ static __device__ __noinline__ unsigned long long hist_gene(
     return tref;
 }
 
-template <class V, int NT, bool ACC_SMEM>
+// HIST: the variant with the histogram path (launched when some column of the launch's tasks
+// can hold small integers; without it the bucket path keeps its register allocation).
+template <class V, int NT, bool ACC_SMEM, bool HIST>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1015,10 +1097,14 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         int nbl = 1;
         while (nbl < a.nb_max_log2 && (1u << nbl) < 2u * nraw) ++nbl;
         const int NB = 1 << nbl;
-        int shift = 0;
-        if (kmin <= kmax) {
-            const int bl = bit_length(K(kmax - kmin));
-            shift = bl > nbl ? bl - nbl : 0;
+        // bucket map: the key map ((key - kmin) >> shift) or, for signed float genes, the signed
+        // map, whose constants the instantiations below rebuild where they need them
+        const bool vmap = BucketMap<V>::signed_range(kmin, kmax);
+        int shift;
+        {
+            BucketMap<V> bm;
+            bm.setup(kmin, kmax, nbl);
+            shift = bm.shift;
         }
         // (the bucket table is all zeros here: zeroed before the first gene, and each gene
         // clears the entries it used while it finalizes)
@@ -1027,7 +1113,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         int hV = 0, hVp = 0;
         long long hv0 = 0;
         bool use_hist = false;
-        if constexpr (ACC_SMEM) {
+        if constexpr (ACC_SMEM && HIST) {
             if (!a.no_histogram && !(s_next_hz & 2u) && kmin <= kmax) {
                 hv0 = (long long)Val<V>::from_key(kmin);
                 use_hist = hist_choice(hv0, (long long)Val<V>::from_key(kmax), G, nraw,
@@ -1035,13 +1121,18 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             }
         }
         unsigned long long tref = 0ull;
-        if (use_hist) {
+        if (HIST && use_hist) {
             tref = hist_gene<V, NT, GT>(hall, hV, hVp, hv0, G, zh, nraw, rows, data, gidp, nrows,
                                         acc, nz, ng, s_wsx, pv_tk, pv_c, &s_pvq, a.erfc_table);
         } else {
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
-        {
+        // (instantiated for each bucket map, chosen once per gene)
+        auto pass1 = [&](auto vm_tag) {
+            constexpr bool VM = decltype(vm_tag)::value;
+            BucketMap<V> bmap;
+            if constexpr (VM) bmap.setup(kmin, kmax, nbl);
+            else { bmap.base = kmin; bmap.shift = shift; }
             uint32_t t = 128u * (uint32_t)warp;
             if (t < nraw) {
                 int32_t r[4];
@@ -1080,7 +1171,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                             if (g) red_add<ACC_SMEM>(&nz[g], 1u);
                             else ++nref_local;
                             if (zh == ZH_MIX && Val<V>::neg(v[k])) red_add<ACC_SMEM>(&ng[g], 1u);
-                            const uint32_t b = (uint32_t)((key - kmin) >> shift);
+                            const uint32_t b = bmap.template at<VM>(key);
                             red_add<true>(&hall[b], 1u);
                             if (g == 0) red_add<true>(&href[b], 1u);
                         }
@@ -1091,13 +1182,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                     for (int k = 0; k < 4; ++k) { r[k] = rn[k]; v[k] = vn[k]; }
                 }
             }
-        }
+        };
+        if (vmap) pass1(std::true_type{});
+        else pass1(std::false_type{});
         nref_local = __reduce_add_sync(0xffffffffu, nref_local);
         if (lane == 0 && nref_local) red_add<ACC_SMEM>(&nz[0], nref_local);
         __syncthreads();
         block_scan2<NT>(hall, href, NB, s_wsx, s_wsy, &s_maxb);
         const uint32_t n = hall[NB];
-        const bool compact = shift <= 16;
+        // 16-bit key offsets inside a bucket: the buckets of the key map hold keys that differ
+        // in their low `shift` bits only
+        const bool compact = !vmap && shift <= 16;
         const uint32_t cap = compact ? cap_compact : cap_full;
         const K offmask = compact ? (K)((1u << shift) - 1u) : K(0);
         // slabs: the whole gene when it fits in shared memory; else buckets whose start lies
@@ -1138,7 +1233,11 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             const bool in_smem = cnt_slab <= cap;
 
             // ---- pass 2 (L2): scatter this slab's decoded elements into bucket order ----
-            if (cnt_slab) {
+            auto scatter = [&](auto vm_tag) {
+                constexpr bool VM = decltype(vm_tag)::value;
+                BucketMap<V> bmap;
+                if constexpr (VM) bmap.setup(kmin, kmax, nbl);
+                else { bmap.base = kmin; bmap.shift = shift; }
                 const bool all = nslabs == 1u;
                 uint32_t t = 128u * (uint32_t)warp;
                 if (t < nraw) {
@@ -1165,7 +1264,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                         bool in[4];
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
-                            bb[k] = (uint32_t)((k4[k] - kmin) >> shift);
+                            bb[k] = bmap.template at<VM>(k4[k]);
                             in[k] = g4[k] != kNoGroup && (all || (bb[k] >= blo && bb[k] < bhi));
                         }
                         uint32_t pos[4];
@@ -1185,6 +1284,10 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                         for (int k = 0; k < 4; ++k) { k4[k] = kn[k]; g4[k] = gn[k]; }
                     }
                 }
+            };
+            if (cnt_slab) {
+                if (vmap) scatter(std::true_type{});
+                else scatter(std::false_type{});
             }
             __syncthreads();
             if (slab + 1u == nslabs) {

@@ -309,7 +309,10 @@ struct ExactArgs {
     // table lookup: pair index of the test's (n1, n2), via a dense map over (n1, n2) when
     // zero_handling != none (per target), else via per-test pair ids
     const int32_t* pair_of_target;  // [T]  (zero_handling != none)
-    const int32_t* pair_of_test;    // [T * n_cols] (zero_handling = none)
+    const int32_t* pair_of_test;    // [T * n_cols] (zero_handling = none, host-built map)
+    const int32_t* pair_index;      // zero_handling = none: pair of (n1, n2) at n1 * pair_w + n2
+    int32_t pair_w;                 //   (when non-null; built from exact_mark_pairs_kernel)
+    int32_t pair_h;
     const long long* pair_n1;
     const long long* pair_n2;
     const long long* offset;
@@ -333,13 +336,31 @@ __device__ __forceinline__ double table_sf(const double* pmf, long long umax, do
     return __ddiv_rn(cdf_small, total);
 }
 
+// zero_handling none: marks the (n1, n2) cells of a dense H x W map that occur among the tests
+// (sample sizes outside the map only come with duplicate row ids, which the run reports)
+__global__ void exact_mark_pairs_kernel(const uint32_t* n1g, const uint32_t* n2t, long long n,
+                                        int32_t n_cols, int32_t H, int32_t W, unsigned char* mark) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t n1 = n1g[i % n_cols], n2 = n2t[i];
+        if (n1 < (uint32_t)H && n2 < (uint32_t)W) mark[(size_t)n1 * W + n2] = 1;
+    }
+}
+
 __global__ void mwu_pvalue_exact_kernel(const ExactArgs a) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
         const int t = (int)(i / a.n_cols);
         int pi;
-        if (a.zero_handling == ZH_NONE) pi = a.pair_of_test[i];
-        else pi = a.pair_of_target[t];
+        if (a.zero_handling != ZH_NONE) {
+            pi = a.pair_of_target[t];
+        } else if (a.pair_index) {
+            const uint32_t n1 = a.n1g[i % a.n_cols], n2 = a.n2t[i];
+            pi = (n1 < (uint32_t)a.pair_h && n2 < (uint32_t)a.pair_w)
+                     ? a.pair_index[(size_t)n1 * a.pair_w + n2] : -1;
+        } else {
+            pi = a.pair_of_test[i];
+        }
         const double U1 = a.U1[i];
         double p = 1.0;
         if (pi >= 0) {

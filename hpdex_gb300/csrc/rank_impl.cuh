@@ -9,25 +9,32 @@ namespace hpdex {
 
 cudaError_t HPDEX_CAT(rank_launch_, HPDEX_RANK_T)(const RankArgs& a, int grid, size_t smem,
                                                   cudaStream_t s) {
-    auto k = a.acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true>
-                           : mwu_rank_kernel<HPDEX_RANK_V, 1024, false>;
+    auto k = !a.acc_in_smem   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>
+             : a.no_histogram ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false>
+                              : mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>;
     k<<<grid, 1024, smem, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t HPDEX_CAT(rank_occupancy_, HPDEX_RANK_T)(size_t smem, size_t smem_optin,
                                                      int acc_in_smem, int* blocks) {
-    auto k = acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true>
-                         : mwu_rank_kernel<HPDEX_RANK_V, 1024, false>;
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k);
-    if (e != cudaSuccess) return e;
-    // the opt-in limit covers static + dynamic shared memory
-    const int max_dyn = (int)(smem_optin - fa.sharedSizeBytes);
-    if ((size_t)max_dyn < smem) return cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k, 1024, smem);
+    // both variants of an accumulator layout get the same shared-memory limit
+    decltype(&mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>) ks[2] = {
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>};
+    for (auto k : ks) {
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, k);
+        if (e != cudaSuccess) return e;
+        // the opt-in limit covers static + dynamic shared memory
+        const int max_dyn = (int)(smem_optin - fa.sharedSizeBytes);
+        if ((size_t)max_dyn < smem) return cudaErrorInvalidValue;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, ks[0], 1024, smem);
 }
 
 }  // namespace hpdex

@@ -115,3 +115,31 @@ def test_drain_wait_fallback_gives_identical_results(fused):
         plan.close()
     finally:
         M.close()
+
+
+def _signed_wide(rng):
+    """Both signs over 60 decades, with subnormals, ties and values next to the signed bucket
+    map's linear/log junction (signed powers of two)."""
+    def f(k):
+        v = rng.standard_normal(k) * 10.0 ** rng.uniform(-30, 30, k)
+        v[rng.random(k) < 0.05] = 1e-42
+        v[rng.random(k) < 0.1] = -3.0
+        p2 = rng.random(k) < 0.1
+        v[p2] = np.ldexp(1.0, rng.integers(-20, 20, int(p2.sum()))) * rng.choice([-1.0, 1.0], int(p2.sum()))
+        return v
+    return f
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("zh", ["min", "none", "mix"])
+def test_signed_wide_range_columns_match_oracle(dtype, zh):
+    """Genes whose values take both signs use the signed bucket map (linear near zero,
+    logarithmic beyond); the results must not depend on it."""
+    rng = np.random.default_rng(17)
+    cols = [(1.0, lambda r: (lambda k: r.standard_normal(k))),
+            (0.9, _signed_wide),
+            (1.0, lambda r: (lambda k: np.round(r.standard_normal(k) * 40) / 40)),
+            (0.6, lambda r: (lambda k: r.standard_normal(k) * 1e-3 + (r.random(k) < 0.01) * 1e4))]
+    w = _workload(23, 60_000, cols, 8_000, [300, 900, 2500, 40, 7000, 1200])
+    w.data = w.data.astype(dtype)
+    assert _oracle_compare(w, zero_handling=zh) == "ok"
