@@ -94,6 +94,7 @@ EXPORTS = {
     "hpdex_plan_set_fused_pvalues": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_set_drain_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_set_histogram": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "hpdex_plan_set_bucket_bits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                           ctypes.POINTER(ctypes.c_int32)]),
     "hpdex_mannwhitneyu_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,

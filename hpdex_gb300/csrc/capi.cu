@@ -385,6 +385,7 @@ struct hpdex_plan {
     DevBuf<uint32_t> cnt;
     RankArgs ra{};
     bool hist_on = true;         // histogram path allowed (hpdex_plan_set_histogram)
+    int nbl = 13;                // bucket table of 2^nbl entries (hpdex_plan_set_bucket_bits)
     bool fused_pvalues = false;  // asymptotic p-values computed inside the rank kernel
     size_t rank_smem = 0;
     int rank_grid = 0;
@@ -644,8 +645,10 @@ struct RankLayout {
     size_t cnt_words(int G) const { return (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G); }
 };
 
-int rank_layout(const DeviceInfo& dev, int dtype, int G, long long max_col, RankLayout* out) {
+int rank_layout(const DeviceInfo& dev, int dtype, int G, long long max_col, RankLayout* out,
+                int nbl = 13) {
     RankLayout r;
+    r.nbl = nbl;
     r.kb = key_bytes(dtype);
     const size_t budget = std::min(dev.smem_per_sm - dev.smem_reserved, dev.smem_optin) - 2048;
     // accumulators and run counters live together: both in shared memory, or both global
@@ -695,7 +698,7 @@ int configure_rank(hpdex_plan* p) {
     const hpdex_matrix* m = p->m;
     const int G = (int)p->G;
     RankLayout r;
-    TRY(rank_layout(m->dev, m->dtype, G, m->max_col_nnz, &r));
+    TRY(rank_layout(m->dev, m->dtype, G, m->max_col_nnz, &r, p->nbl));
     p->rank_smem = r.smem;
     p->rank_grid = r.grid;
     TRY(p->dk.alloc(r.dk_bytes()));
@@ -1430,6 +1433,26 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
     if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
     return HPDEX_OK;
+}
+
+int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (bits < 9 || bits > 13) return fail(HPDEX_ERR_ARGUMENT, "bucket bits must be in [9, 13]");
+    if (bits == p->nbl) return HPDEX_OK;
+    const int old = p->nbl;
+    const RankArgs keep = p->ra;  // the plan's other launch settings stay as they were
+    p->nbl = bits;
+    int st = configure_rank(p);
+    if (st != HPDEX_OK) {
+        p->nbl = old;
+        configure_rank(p);
+    }
+    p->ra.erfc_table = keep.erfc_table;
+    p->ra.no_drain_wait = keep.no_drain_wait;
+    p->ra.no_histogram = keep.no_histogram;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return st;
 }
 
 int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on) {

@@ -951,6 +951,47 @@ static __device__ __noinline__ unsigned long long hist_gene(
     return tref;
 }
 
+// Finalize of one gene (threads take targets 1 + tid, 1 + tid + NT, ...): the zero block,
+// U1 and the (masked) tie sum per target from the accumulators A (doubled U2 terms of the
+// stored elements), B (target tie terms), the stored counts nz and negatives ng, and T_ref;
+// zero_handling none also writes the per-test sample sizes. Sample-size errors and duplicate
+// row ids go to the task's error words (lowest gene * G + group wins).
+template <int NT>
+__device__ __forceinline__ void finalize_gene(const RankTask* tk, int c, int G, int zh, const Acc& acc,
+                                              const uint32_t* nz, const uint32_t* ng,
+                                              unsigned long long T_ref) {
+    const unsigned long long nz1 = nz[0];
+    for (int g = 1 + (int)threadIdx.x; g < G; g += NT) {
+        const size_t idx = (size_t)(g - 1) * tk->n_cols + c;
+        const unsigned long long nz2 = nz[g];
+        unsigned long long n1, n2, u2x2, ties;
+        if (zh == ZH_NONE) {
+            n1 = nz1;
+            n2 = nz2;
+            if (n1 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G);
+            else if (n2 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G + g);
+            u2x2 = acc.A[g];
+            ties = T_ref + acc.B[g];
+            tk->n2[idx] = (uint32_t)nz2;
+            if (g == 1) tk->n1[c] = (uint32_t)nz1;
+        } else {
+            n1 = (unsigned long long)tk->group_rows[0];
+            n2 = (unsigned long long)tk->group_rows[g];
+            if (nz1 > n1) atomicMin(&tk->err[1], (unsigned long long)c * G);
+            if (nz2 > n2) atomicMin(&tk->err[1], (unsigned long long)c * G + g);
+            const unsigned long long z1 = n1 - nz1, z2 = n2 - nz2;
+            if (zh == ZH_MIN) u2x2 = acc.A[g] + 2ull * z1 * nz2 + z1 * z2;
+            else if (zh == ZH_MAX) u2x2 = acc.A[g] + z2 * (2ull * nz1 + z1);
+            else u2x2 = acc.A[g] + 2ull * z1 * (nz2 - ng[g]) + z2 * (2ull * ng[0] + z1);
+            const unsigned long long zz = z1 + z2;
+            ties = T_ref + acc.B[g] + zz * zz * zz - zz;
+        }
+        const long long u1x2 = (long long)(2ull * n1 * n2) - (long long)u2x2;
+        tk->U1[idx] = (double)u1x2 * 0.5;
+        tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
+    }
+}
+
 // HIST: the variant with the histogram path (launched when some column of the launch's tasks
 // can hold small integers; without it the bucket path keeps its register allocation).
 template <class V, int NT, bool ACC_SMEM, bool HIST>
@@ -1326,37 +1367,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         // the s_next_* values of this gene were read after the barriers above; the next gene
         // is fetched now (thread NT - 1 finalizes a target only when G > NT)
         if (tid == NT - 1) fetch_next();
-        const unsigned long long T_ref = s_tref;
-        const unsigned long long nz1 = nz[0];
-        for (int g = 1 + tid; g < G; g += NT) {
-            const size_t idx = (size_t)(g - 1) * tk->n_cols + c;
-            const unsigned long long nz2 = nz[g];
-            unsigned long long n1, n2, u2x2, ties;
-            if (zh == ZH_NONE) {
-                n1 = nz1;
-                n2 = nz2;
-                if (n1 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G);
-                else if (n2 < 2) atomicMin(&tk->err[0], (unsigned long long)c * G + g);
-                u2x2 = A[g];
-                ties = T_ref + B[g];
-                tk->n2[idx] = (uint32_t)nz2;
-                if (g == 1) tk->n1[c] = (uint32_t)nz1;
-            } else {
-                n1 = (unsigned long long)tk->group_rows[0];
-                n2 = (unsigned long long)tk->group_rows[g];
-                if (nz1 > n1) atomicMin(&tk->err[1], (unsigned long long)c * G);
-                if (nz2 > n2) atomicMin(&tk->err[1], (unsigned long long)c * G + g);
-                const unsigned long long z1 = n1 - nz1, z2 = n2 - nz2;
-                if (zh == ZH_MIN) u2x2 = A[g] + 2ull * z1 * nz2 + z1 * z2;
-                else if (zh == ZH_MAX) u2x2 = A[g] + z2 * (2ull * nz1 + z1);
-                else u2x2 = A[g] + 2ull * z1 * (nz2 - ng[g]) + z2 * (2ull * ng[0] + z1);
-                const unsigned long long zz = z1 + z2;
-                ties = T_ref + B[g] + zz * zz * zz - zz;
-            }
-            const long long u1x2 = (long long)(2ull * n1 * n2) - (long long)u2x2;
-            tk->U1[idx] = (double)u1x2 * 0.5;
-            tk->tie[idx] = tk->tie_correction ? (double)ties : 0.0;
-        }
+        finalize_gene<NT>(tk, c, G, zh, acc, nz, ng, s_tref);
         // for the next gene: a clear bucket table (all of it, and the big list, after the
         // histogram path used the region for its counters)
         const int nb_used = use_hist ? NBMAX : NB;

@@ -140,6 +140,11 @@ class Plan:
         """Asymptotic p-values inside the rank kernel (default) or in a separate kernel."""
         _lib.check(_lib.lib().hpdex_plan_set_fused_pvalues(self._h, int(bool(on))))
 
+    def set_bucket_bits(self, bits: int) -> None:
+        """Diagnostic: the rank kernel's bucket table of 2**bits entries (9..13); the results do
+        not change."""
+        _lib.check(_lib.lib().hpdex_plan_set_bucket_bits(self._h, int(bits)))
+
     def set_histogram(self, on: bool) -> None:
         """Per-gene histogram path for small-integer values (default) or the bucket path for
         every gene; the results are the same."""

@@ -213,6 +213,11 @@ int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on);
 /* Copies U1 / P (n_targets x n_cols, target-major) to host; either pointer may be NULL. */
 int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
 
+/* Diagnostic: the rank kernel's bucket table of 2^bits entries (9..13; 13, the default, was
+ * the fastest on every workload measured). A smaller table leaves more shared memory for a
+ * gene's elements at the cost of larger buckets. The results do not depend on it. */
+int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits);
+
 /* The rank kernel takes each gene whose stored values are integers of magnitude below 2^31
  * (UMI counts) and whose value span times the number of groups fits its shared memory through
  * a histogram path: one counter per (value, group), rank sums from a prefix scan of the

@@ -143,3 +143,25 @@ def test_signed_wide_range_columns_match_oracle(dtype, zh):
     w = _workload(23, 60_000, cols, 8_000, [300, 900, 2500, 40, 7000, 1200])
     w.data = w.data.astype(dtype)
     assert _oracle_compare(w, zero_handling=zh) == "ok"
+
+
+def test_bucket_table_size_does_not_change_results():
+    """The bucket table (2^9 .. 2^13 entries) only changes the work split: smaller tables mean
+    larger buckets and more elements per slab. U1 and P stay the same doubles."""
+    from hpdex_gb300.resident import BATCHED, ResidentMatrix
+    sizes = [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]
+    w = _workload(3, 150_000, COLUMNS, 30_000, sizes)
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    try:
+        plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        plan.run(BATCHED)
+        U1a, Pa = plan.download()
+        for bits in (12, 10, 9, 13):
+            plan.set_bucket_bits(bits)
+            plan.run(BATCHED)
+            U1b, Pb = plan.download()
+            np.testing.assert_array_equal(U1b, U1a)
+            np.testing.assert_array_equal(Pb, Pa)
+        plan.close()
+    finally:
+        M.close()
