@@ -491,8 +491,19 @@ def run_ours(args, rank, world):
                               "value": tests / statistics.median(ts),
                               "median_ms": statistics.median(ts) * 1e3}), flush=True)
         return 0
+    if args.only_batched and args.workload != "screen":
+        # profiling runs on the other workloads: the batched plan only
+        from hpdex_gb300 import synthetic
+        w = synthetic.umi_counts() if args.workload == "umi" else synthetic.exact_small()
+        T, C = w.n_targets, w.n_cols
+        tests = T * C
+        opt = (dict(zero_handling="min", use_continuity=True, tie_correction=True)
+               if args.workload == "umi" else
+               dict(zero_handling="none", use_continuity=False, tie_correction=True, method="exact"))
+    else:
+        opt = dict(zero_handling="min", use_continuity=True, tie_correction=True)
     M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
-    plan = M.plan(w.group_id, T, zero_handling="min", use_continuity=True, tie_correction=True)
+    plan = M.plan(w.group_id, T, **opt)
     if args.only_batched and args.separate_pvalues:
         plan.set_fused_pvalues(False)
     sampler = clock_sampler()  # sampling from before the warm-up on
@@ -681,6 +692,9 @@ def main():
                     help="time the public one-shot call only (for ncu)")
     ap.add_argument("--separate-pvalues", action="store_true",
                     help="with --only-batched: p-values in a separate kernel (for ncu)")
+    ap.add_argument("--workload", choices=["screen", "umi", "exact"], default="screen",
+                    help="with --only-batched: the 200k x 8k screen (default), the 50k x 2k "
+                         "integer-count workload or the 60k x 4k exact-mode workload (for ncu)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 3 if args.impl == "reference" else 300
