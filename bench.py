@@ -23,11 +23,14 @@ One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
           per-gene histogram path against the bucket path only, group means, CPU port.
   exact : the 60,000 x 4,000 dense exact-mode workload (40 reference cells, 1,500 targets):
           both DP variants on the device, CPU port on a gene sample.
-  serving: the serving loop (hpdex_gb300.serving) over three resident matrices (the
-          200k x 8k screen, a 50k x 2k log1p-CP10k matrix and a 50k x 2k integer-count
-          matrix), Poisson arrivals of random groupings (reference 1k-50k cells, 1-200
-          targets of 20-5,000 cells), p50/p99 latency and tests/s, coalesced launches
-          (max_batch=16) against per-query launches (max_batch=1), at two arrival rates.
+  serving: the serving loop (hpdex_gb300.serving) over five resident matrices (the
+          200k x 8k screen, a 50k x 2k log1p-CP10k matrix, a 50k x 2k integer-count matrix,
+          and a 1M x 20k log1p-CP10k atlas of 1e9 entries generated on the GPU with its
+          integer-count twin; 70 % float / 30 % count queries), Poisson arrivals of random
+          groupings (reference 1k-50k cells, 1-200 targets of 20-5,000 cells), p50/p99 latency
+          overall and per matrix, tests/s, per-phase device time, coalesced launches
+          (max_batch=16) against per-query launches (max_batch=1), at a sustained and a
+          saturating arrival rate.
 The inputs (1.17 GB resident) exceed the 129 MB L2, so no flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference backend (oracle/, OpenMP over all
@@ -324,31 +327,52 @@ def run_reference(args, rank, world):
     return 0
 
 
-def serving_leg(M, w, queries=150, rates=(300.0, 1500.0)):
-    """Serving loop on the resident screen plus two 50k x 2k matrices (see module doc)."""
+def serving_leg(M, w, queries=120, rates=(40.0, 2000.0)):
+    """Serving loop over five resident matrices (see module doc): the screen, a 50k x 2k
+    log1p-CP10k matrix, an integer-count 50k x 2k matrix, and the 1M x 20k atlas
+    (1e9 entries, generated on the GPU) with its integer-count twin. 70 % of the queries go to
+    the float matrices, 30 % to the integer-count ones. Arrivals are Poisson at a sustained
+    rate and at a saturating one, with coalesced (max_batch 16) and per-query launches."""
     from hpdex_gb300 import synthetic
     from hpdex_gb300.resident import ResidentMatrix
     from hpdex_gb300.serving import Server, poisson_run
     b = synthetic.perturb_screen(seed=3, n_rows=50_000, n_cols=2_000, n_targets=50, ref_size=5_000)
     c = synthetic.umi_counts(seed=4, n_rows=50_000, n_cols=2_000)
+    t_gen = time.perf_counter()
+    atlas, atlas_counts = synthetic.resident_atlas()
+    t_gen = time.perf_counter() - t_gen
     mats = [M, ResidentMatrix(b.data, b.indices, b.indptr, b.n_rows),
-            ResidentMatrix(c.data, c.indices, c.indptr, c.n_rows)]
-    rows = {0: w.n_rows, 1: b.n_rows, 2: c.n_rows}
+            ResidentMatrix(c.data, c.indices, c.indptr, c.n_rows), atlas, atlas_counts]
+    names = ["screen 200000x8000 float", "50000x2000 float", "50000x2000 counts",
+             "atlas 1000000x20000 float", "atlas 1000000x20000 counts"]
+    rows = {0: w.n_rows, 1: b.n_rows, 2: c.n_rows, 3: atlas.n_rows, 4: atlas_counts.n_rows}
+    weights = [0.7 / 3, 0.7 / 3, 0.3 / 2, 0.7 / 3, 0.3 / 2]
     runs = []
     for mode, mb in (("coalesced", 16), ("per_query", 1)):
         for rate in rates:
-            with Server(workspace_bytes=32 << 30, max_batch=mb) as srv:
+            with Server(workspace_bytes=64 << 30, max_batch=mb) as srv:
                 ids = [srv.add_matrix(m) for m in mats]
-                poisson_run(srv, ids, rows, rate_qps=rate, n_queries=20, seed=1)  # warm-up
-                r = poisson_run(srv, ids, rows, rate_qps=rate, n_queries=queries, seed=2)
+                poisson_run(srv, ids, rows, rate_qps=rate, n_queries=10, seed=1, weights=weights)
+                base = srv.stats()
+                r = poisson_run(srv, ids, rows, rate_qps=rate, n_queries=queries, seed=2,
+                                weights=weights)
             runs.append({"mode": mode, "max_batch": mb, "rate_qps": rate,
                          "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "mean_ms": r["mean_ms"],
-                         "tests_per_s": r["tests_per_s"], "launches": r["batches"],
-                         "gpu_busy_ms": r["busy_ms"]})
-    return {"matrices": "200000x8000 screen (1.47e8 nnz), 50000x2000 log1p-CP10k, "
-                        "50000x2000 integer counts; all resident float32",
-            "queries_per_run": queries, "arrival": "Poisson", "runs": runs,
-            "note": "latency = submit to results in host memory; tests/s over the run's wall time"}
+                         "tests_per_s": r["tests_per_s"], "launches": r["batches"] - base["batches"],
+                         "gpu_busy_ms": r["busy_ms"] - base["busy_ms"],
+                         "phase_ms": {"host_prep": r["prep_ms"] - base["prep_ms"],
+                                      "rank": r["rank_ms"] - base["rank_ms"],
+                                      "pvalue": r["pvalue_ms"] - base["pvalue_ms"]},
+                         "per_matrix": {names[k]: v for k, v in r["per_matrix"].items()}})
+    atlas.close()
+    atlas_counts.close()
+    return {"matrices": names, "atlas_nnz": 1_000_000_000, "atlas_generation_s": t_gen,
+            "query_mix": "70 % float / 30 % integer counts", "queries_per_run": queries,
+            "arrival": "Poisson", "rates": {"sustained_qps": rates[0], "saturating_qps": rates[1]},
+            "runs": runs,
+            "note": "latency = submit to results in host memory; tests/s over the run's wall time; "
+                    "phase_ms = host preparation of the batches, device time of the rank and "
+                    "p-value launches (one p-value launch per batch)"}
 
 
 def time_plan(plan, steps, warmup=2):

@@ -75,6 +75,9 @@ EXPORTS = {
     "hpdex_matrix_create_idx32": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                            ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "hpdex_matrix_create_device": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                                  ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "hpdex_matrix_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "hpdex_matrix_create_csr": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
@@ -115,6 +118,9 @@ EXPORTS = {
     "hpdex_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                           ctypes.POINTER(ctypes.c_int64),
                                           ctypes.POINTER(ctypes.c_double)]),
+    "hpdex_server_phase_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double)]),
     "hpdex_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }
 

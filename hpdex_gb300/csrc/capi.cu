@@ -552,13 +552,14 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
     TRY(m->data.alloc(std::max<size_t>(1, (size_t)m->nnz * vs)));
     TRY(m->rows.alloc(std::max<long long>(1, m->nnz)));
     TRY(m->indptr.alloc((size_t)m->n_cols + 1));
-    if (m->nnz) CUDA_TRY(cudaMemcpy(m->data.p, data, (size_t)m->nnz * vs, cudaMemcpyHostToDevice));
+    // values and int32 row ids may be host or device memory (hpdex_matrix_create_device)
+    if (m->nnz) CUDA_TRY(cudaMemcpy(m->data.p, data, (size_t)m->nnz * vs, cudaMemcpyDefault));
     CUDA_TRY(cudaMemcpy(m->indptr.p, indptr, sizeof(int64_t) * ((size_t)m->n_cols + 1),
                         cudaMemcpyHostToDevice));
     // row ids: int64 -> int32 through a bounded staging buffer
     const long long chunk = 1ll << 24;
     if (m->nnz && indices32) {
-        CUDA_TRY(cudaMemcpy(m->rows.p, indices32, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(m->rows.p, indices32, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyDefault));
     } else if (m->nnz) {
         DevBuf<long long> stage;
         TRY(stage.alloc((size_t)std::min(chunk, m->nnz)));
@@ -1258,6 +1259,12 @@ int hpdex_matrix_create_idx32(int32_t dtype, const void* data, const int32_t* in
     return matrix_create(dtype, data, nullptr, indices, indptr, n_rows, n_cols, nnz, out);
 }
 
+int hpdex_matrix_create_device(int32_t dtype, const void* d_data, const int32_t* d_rows,
+                               const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                               hpdex_matrix** out) {
+    return matrix_create(dtype, d_data, nullptr, d_rows, indptr, n_rows, n_cols, nnz, out);
+}
+
 int hpdex_matrix_destroy(hpdex_matrix* m) {
     delete m;
     return HPDEX_OK;
@@ -1946,7 +1953,8 @@ struct ServerQuery {
     int matrix = 0;
     long long T = 0, G = 0;
     hpdex_mwu_options opt{};
-    std::vector<int32_t> gid;
+    std::vector<int32_t> gid;      // group ids (when no page-locked buffer was free)
+    int32_t* gid_pinned = nullptr; // group ids in a page-locked pool buffer (asynchronous copy)
     std::vector<long long> group_rows;
     double* U1_out = nullptr;
     double* P_out = nullptr;
@@ -1963,6 +1971,9 @@ struct ServerQuery {
     int status = -1;      // -1 while pending or running
     std::string error;
     std::chrono::steady_clock::time_point t_submit, t_done;
+    ~ServerQuery() {
+        if (gid_pinned) host_pool().put(gid_pinned);
+    }
 };
 
 struct ServerBatch {
@@ -1972,9 +1983,14 @@ struct ServerBatch {
     DevBuf<uint16_t> order_task;
     DevBuf<unsigned char> dk, dg, ek, eg, acc;
     DevBuf<uint32_t> cnt;
-    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    DevBuf<PArgs> psets;       // the batch's p-value sets (one launch for all queries)
+    DevBuf<long long> pfirst;
+    // device time: t0 before the rank launch, tr after it, t1 after the p-values
+    cudaEvent_t t0 = nullptr, tr = nullptr, t1 = nullptr;
+    double prep_ms = 0.0;      // host time to prepare and queue the batch
     ~ServerBatch() {
         if (t0) cudaEventDestroy(t0);
+        if (tr) cudaEventDestroy(tr);
         if (t1) cudaEventDestroy(t1);
     }
 };
@@ -1986,6 +2002,12 @@ struct hpdex_server {
     int max_batch = 1;
     DeviceInfo dev;
     std::vector<hpdex_matrix*> mats;
+    // per matrix: its genes in descending nnz, and the segment of that order holding each nnz
+    // class floor(log2(nnz + 1)) = k: [seg[2k], seg[2k + 1]). A batch's work queue takes the
+    // classes in descending order, each with every query's genes of that class: longest first
+    // within a factor of two, built in time linear in the items (no sort per batch)
+    std::vector<std::vector<int32_t>> mat_order;
+    std::vector<std::vector<int64_t>> mat_class_start;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<ServerQuery*> pending;
@@ -1995,6 +2017,7 @@ struct hpdex_server {
     bool stop = false;
     int64_t completed = 0, batches = 0;
     double busy_ms = 0.0;
+    double rank_ms = 0.0, pvalue_ms = 0.0, prep_ms = 0.0;  // per phase, over all batches
     cudaStream_t stream = nullptr;
     std::thread worker;
 };
@@ -2049,7 +2072,8 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
             TRY(q->n2.alloc((size_t)std::max<long long>(tc, 1)));
         }
         TRY(q->err.alloc(kErrWords));
-        if (R) CUDA_TRY(cudaMemcpyAsync(q->d_gid.p, q->gid.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
+        if (R) CUDA_TRY(cudaMemcpyAsync(q->d_gid.p, q->gid_pinned ? q->gid_pinned : q->gid.data(),
+                                        sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemcpyAsync(q->d_group_rows.p, q->group_rows.data(), sizeof(long long) * q->G, cudaMemcpyHostToDevice, st));
         q->pconst = target_consts(q->group_rows, q->opt.zero_handling);
         if (!q->pconst.empty()) {
@@ -2084,20 +2108,19 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         t.n2 = q->n2.p;
         t.err = q->err.p;
     }
-    // one longest-first queue over every (query, gene) item of the batch
-    std::vector<std::pair<long long, int64_t>> it;
-    it.reserve((size_t)items);
-    for (size_t i = 0; i < b.q.size(); ++i) {
-        const hpdex_matrix* m = S->mats[(size_t)b.q[i]->matrix];
-        for (long long c = 0; c < m->n_cols; ++c) it.push_back({m->col_nnz[(size_t)c], ((int64_t)i << 32) | c});
-    }
-    std::stable_sort(it.begin(), it.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-    std::vector<int32_t> order(it.size());
-    std::vector<uint16_t> order_task(it.size());
-    for (size_t k = 0; k < it.size(); ++k) {
-        order[k] = (int32_t)(it[k].second & 0xffffffff);
-        order_task[k] = (uint16_t)(it[k].second >> 32);
-    }
+    // one work queue over every (query, gene) item of the batch, longest first by nnz class
+    std::vector<int32_t> order;
+    std::vector<uint16_t> order_task;
+    order.reserve((size_t)items);
+    order_task.reserve((size_t)items);
+    for (int k = 63; k >= 0; --k)
+        for (size_t i = 0; i < b.q.size(); ++i) {
+            const auto& ord = S->mat_order[(size_t)b.q[i]->matrix];
+            const auto& seg = S->mat_class_start[(size_t)b.q[i]->matrix];
+            const int64_t lo = seg[(size_t)(2 * k)], hi = seg[(size_t)(2 * k + 1)];
+            order.insert(order.end(), ord.begin() + lo, ord.begin() + hi);
+            order_task.insert(order_task.end(), (size_t)(hi - lo), (uint16_t)i);
+        }
     TRY(b.tasks.alloc(tasks.size()));
     TRY(b.order.alloc(std::max<size_t>(order.size(), 1)));
     TRY(b.order_task.alloc(std::max<size_t>(order.size(), 1)));
@@ -2129,6 +2152,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
     }
 
     CUDA_TRY(cudaEventCreate(&b.t0));
+    CUDA_TRY(cudaEventCreate(&b.tr));
     CUDA_TRY(cudaEventCreate(&b.t1));
     CUDA_TRY(cudaEventRecord(b.t0, st));
     if (!order.empty()) {
@@ -2145,6 +2169,10 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         set_layout_args(a, r, GL, b.dk.p, b.dg.p, b.ek.p, b.eg.p, b.acc.p, b.cnt.p);
         TRY(rank_status(rank_launch(dtype, a, r.grid, r.smem, st), "rank kernel launch"));
     }
+    CUDA_TRY(cudaEventRecord(b.tr, st));
+    // the p-values of every query of the batch: one launch
+    std::vector<PArgs> sets;
+    std::vector<long long> first{0};
     for (ServerQuery* q : b.q) {
         const hpdex_matrix* m = S->mats[(size_t)q->matrix];
         PArgs pa{};
@@ -2164,11 +2192,17 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         pa.alternative = q->opt.alternative;
         pa.cc = q->opt.use_continuity ? 0.5 : 0.0;
         pa.fast = q->opt.fast_norm;
-        if (pa.n) {
-            const int grid = (int)std::min<long long>((pa.n + 255) / 256, (long long)S->dev.sms * 8);
-            mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, st>>>(pa);
-            CUDA_TRY(cudaGetLastError());
-        }
+        sets.push_back(pa);
+        first.push_back(first.back() + pa.n);
+    }
+    if (first.back() > 0) {
+        TRY(b.psets.alloc(sets.size()));
+        TRY(b.pfirst.alloc(first.size()));
+        CUDA_TRY(cudaMemcpyAsync(b.psets.p, sets.data(), sizeof(PArgs) * sets.size(), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(b.pfirst.p, first.data(), sizeof(long long) * first.size(), cudaMemcpyHostToDevice, st));
+        const int grid = (int)std::min<long long>((first.back() + 255) / 256, (long long)S->dev.sms * 8);
+        mwu_pvalue_batch_kernel<<<grid, 256, 0, st>>>(b.psets.p, b.pfirst.p, (int)sets.size());
+        CUDA_TRY(cudaGetLastError());
     }
     CUDA_TRY(cudaEventRecord(b.t1, st));
     return HPDEX_OK;
@@ -2176,6 +2210,10 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
 
 // Marks a query finished (caller holds S->mu) and releases its workspace.
 void server_finish_query(hpdex_server* S, ServerQuery* q, int status, const std::string& msg) {
+    if (q->gid_pinned) {  // its upload finished with the batch
+        host_pool().put(q->gid_pinned);
+        q->gid_pinned = nullptr;
+    }
     q->status = status;
     q->error = msg;
     q->t_done = std::chrono::steady_clock::now();
@@ -2194,8 +2232,9 @@ void server_finish_query(hpdex_server* S, ServerQuery* q, int status, const std:
 
 // Results and errors of a finished batch.
 void server_complete(hpdex_server* S, ServerBatch& b) {
-    float ms = 0.0f;
+    float ms = 0.0f, rms = 0.0f;
     cudaEventElapsedTime(&ms, b.t0, b.t1);
+    cudaEventElapsedTime(&rms, b.t0, b.tr);
     std::vector<std::pair<int, std::string>> res;
     for (ServerQuery* q : b.q) {
         unsigned long long e[kErrWords];
@@ -2221,6 +2260,9 @@ void server_complete(hpdex_server* S, ServerBatch& b) {
     for (size_t i = 0; i < b.q.size(); ++i) server_finish_query(S, b.q[i], res[i].first, res[i].second);
     S->batches += 1;
     S->busy_ms += ms;
+    S->rank_ms += rms;
+    S->pvalue_ms += ms - rms;
+    S->prep_ms += b.prep_ms;
     S->cv_done.notify_all();
 }
 
@@ -2273,7 +2315,10 @@ void server_loop(hpdex_server* S) {
             }
         }
         if (!b) continue;
-        if (server_launch(S, *b) != HPDEX_OK) {
+        const auto tp0 = std::chrono::steady_clock::now();
+        const int lst = server_launch(S, *b);
+        b->prep_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tp0).count();
+        if (lst != HPDEX_OK) {
             const std::string msg = hpdex_last_error();
             cudaStreamSynchronize(S->stream);
             std::lock_guard<std::mutex> lock(S->mu);
@@ -2313,8 +2358,26 @@ int hpdex_server_create(int64_t workspace_bytes, int32_t max_batch, hpdex_server
 int hpdex_server_add_matrix(hpdex_server* s, hpdex_matrix* m, int32_t* matrix_id) {
     if (!s || !m || !matrix_id) return fail(HPDEX_ERR_ARGUMENT, "NULL server, matrix or id pointer");
     if (m->dev.device != s->dev.device) return fail(HPDEX_ERR_ARGUMENT, "matrix and server are on different devices");
+    std::vector<int32_t> order((size_t)m->n_cols);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return m->col_nnz[(size_t)a] > m->col_nnz[(size_t)b];
+    });
+    auto cls = [&](int32_t c) {
+        const unsigned long long v = (unsigned long long)m->col_nnz[(size_t)c] + 1ull;
+        return 63 - __builtin_clzll(v);
+    };
+    // classes fall along the descending order: class k is the segment [seg[2k], seg[2k + 1])
+    std::vector<int64_t> seg(128, 0);
+    for (size_t i = 0; i < order.size(); ++i) {
+        const int k = cls(order[i]);
+        if (seg[(size_t)(2 * k + 1)] == 0) seg[(size_t)(2 * k)] = (int64_t)i;
+        seg[(size_t)(2 * k + 1)] = (int64_t)i + 1;
+    }
     std::lock_guard<std::mutex> lock(s->mu);
     s->mats.push_back(m);
+    s->mat_order.push_back(std::move(order));
+    s->mat_class_start.push_back(std::move(seg));
     *matrix_id = (int32_t)(s->mats.size() - 1);
     return HPDEX_OK;
 }
@@ -2341,7 +2404,10 @@ int hpdex_server_submit(hpdex_server* s, int32_t matrix_id, const int32_t* group
     q->T = n_targets;
     q->G = G;
     q->opt = *opt;
-    q->gid.assign(group_id, group_id + R);
+    // a page-locked copy when the pool has one free: the worker's upload is then asynchronous
+    q->gid_pinned = R > 0 ? static_cast<int32_t*>(host_pool().get(sizeof(int32_t) * (size_t)R)) : nullptr;
+    if (q->gid_pinned) std::memcpy(q->gid_pinned, group_id, sizeof(int32_t) * (size_t)R);
+    else q->gid.assign(group_id, group_id + R);
     q->group_rows.assign((size_t)G, 0);
     for (long long r = 0; r < R; ++r) {
         const int g = group_id[r];
@@ -2393,6 +2459,16 @@ int hpdex_server_stats(const hpdex_server* s, int64_t* completed, int64_t* batch
     if (completed) *completed = s->completed;
     if (batches) *batches = s->batches;
     if (busy_ms) *busy_ms = s->busy_ms;
+    return HPDEX_OK;
+}
+
+int hpdex_server_phase_stats(const hpdex_server* s, double* prep_ms, double* rank_ms, double* pvalue_ms) {
+    if (!s) return fail(HPDEX_ERR_ARGUMENT, "server is NULL");
+    hpdex_server* w = const_cast<hpdex_server*>(s);
+    std::lock_guard<std::mutex> lock(w->mu);
+    if (prep_ms) *prep_ms = s->prep_ms;
+    if (rank_ms) *rank_ms = s->rank_ms;
+    if (pvalue_ms) *pvalue_ms = s->pvalue_ms;
     return HPDEX_OK;
 }
 

@@ -874,6 +874,16 @@ __device__ void block_scan1(uint32_t* x, int L, uint32_t* ws) {
     __syncthreads();
 }
 
+// Bin of a small-integer value (|v| < 2^31, as the column flag guarantees) relative to the
+// gene's smallest value: converted in the value's own type, so that float data does not go
+// through double (conversions to and from double take the narrow FP64 pipe).
+template <class V>
+__device__ __forceinline__ uint32_t hist_bin(V v, long long lo) {
+    if constexpr (std::is_same_v<V, float>) return (uint32_t)(__float2int_rz(v) - (int32_t)lo);
+    else if constexpr (std::is_same_v<V, double>) return (uint32_t)(__double2int_rz(v) - (int32_t)lo);
+    else return (uint32_t)((long long)v - lo);
+}
+
 // One gene on the histogram path (hc: the counter region, 16-byte aligned); returns this
 // thread's share of T_ref. Not inlined, so that its registers stay out of the bucket path's
 // allocation. The caller's next block barrier orders its reads of the counters before the
@@ -911,7 +921,7 @@ static __device__ __noinline__ unsigned long long hist_gene(
             const bool ok = gl[k] != kNoGroup && Val<V>::finite(v[k]) &&
                             (zh == ZH_NONE || !Val<V>::zero(v[k]));
             if (ok) {
-                const uint32_t bin = (uint32_t)((long long)Val<V>::to_double(v[k]) - hv0);
+                const uint32_t bin = hist_bin<V>(v[k], hv0);
                 red_add<true>(&hc[(gl[k] ? 4u + gl[k] * (uint32_t)hVp : 0u) + bin], 1u);
             }
         }

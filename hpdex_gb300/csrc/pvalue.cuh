@@ -151,25 +151,44 @@ __device__ __forceinline__ void test_sizes(const PArgs& a, int t, int c, long lo
     }
 }
 
+// the p-value of test i of a's column range
+__device__ __forceinline__ void pvalue_one(const PArgs& a, long long i) {
+    int t, c;
+    const long long idx = test_index(a, i, t, c);
+    double n1, n2;
+    test_sizes(a, t, c, idx, n1, n2);
+    const double u1 = a.U1[idx];
+    double p;
+    if (a.fast) p = p_asymptotic_fast(u1, n1, n2, a.P[idx], a.cc, a.alternative);
+    else if (a.pk && a.zero_handling != ZH_NONE)
+        p = p_asymptotic_k(u1, a.pk[t], a.P[idx], a.cc, a.alternative, g_erfc_table);
+    else p = p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative, g_erfc_table);
+    if (a.P_out) {
+        a.U1_out[idx] = u1;
+        a.P_out[idx] = p;
+    } else {
+        a.P[idx] = p;
+    }
+}
+
 __global__ void mwu_pvalue_asymptotic_kernel(const PArgs a) {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-        int t, c;
-        const long long idx = test_index(a, i, t, c);
-        double n1, n2;
-        test_sizes(a, t, c, idx, n1, n2);
-        const double u1 = a.U1[idx];
-        double p;
-        if (a.fast) p = p_asymptotic_fast(u1, n1, n2, a.P[idx], a.cc, a.alternative);
-        else if (a.pk && a.zero_handling != ZH_NONE)
-            p = p_asymptotic_k(u1, a.pk[t], a.P[idx], a.cc, a.alternative, g_erfc_table);
-        else p = p_asymptotic(u1, n1, n2, a.P[idx], a.cc, a.alternative, g_erfc_table);
-        if (a.P_out) {
-            a.U1_out[idx] = u1;
-            a.P_out[idx] = p;
-        } else {
-            a.P[idx] = p;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
+        pvalue_one(a, i);
+}
+
+// The p-values of several independent test sets in one launch (a batch of the serving loop):
+// set k covers the tests [first[k], first[k + 1]) of the launch.
+__global__ void mwu_pvalue_batch_kernel(const PArgs* sets, const long long* first, int n_sets) {
+    const long long n = first[n_sets];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int lo = 0, hi = n_sets - 1;  // the last set k with first[k] <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= i) lo = mid; else hi = mid - 1;
         }
+        pvalue_one(sets[lo], i - first[lo]);
     }
 }
 

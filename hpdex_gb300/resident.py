@@ -86,6 +86,25 @@ class ResidentMatrix:
         self.nnz = self._info()[2]
         return self
 
+    @classmethod
+    def from_device(cls, data_ptr: int, rows_ptr: int, indptr, n_rows: int, dtype):
+        """A matrix whose values (`dtype`) and int32 row ids are already in device memory at
+        data_ptr / rows_ptr (copied into the library's buffers); indptr is a host array."""
+        self = cls.__new__(cls)
+        dtype = np.dtype(dtype)
+        if dtype.name not in _lib.DTYPE_CODES:
+            raise RuntimeError("Unsupported dtype for data")
+        indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+        self.n_rows, self.n_cols, self.dtype = int(n_rows), indptr.size - 1, dtype
+        self.nnz = int(indptr[-1])
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().hpdex_matrix_create_device(_lib.DTYPE_CODES[dtype.name], int(data_ptr),
+                                                         int(rows_ptr), indptr.ctypes.data,
+                                                         self.n_rows, self.n_cols, self.nnz,
+                                                         ctypes.byref(h)))
+        self._h = h
+        return self
+
     def _info(self):
         v = [ctypes.c_int64() for _ in range(4)]
         _lib.check(_lib.lib().hpdex_matrix_info(self._h, *[ctypes.byref(x) for x in v]))

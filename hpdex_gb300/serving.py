@@ -84,7 +84,11 @@ class Server:
         c, b, ms = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
         _lib.check(_lib.lib().hpdex_server_stats(self._h, ctypes.byref(c), ctypes.byref(b),
                                                  ctypes.byref(ms)))
-        return {"completed": c.value, "batches": b.value, "busy_ms": ms.value}
+        pr, rk, pv = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _lib.check(_lib.lib().hpdex_server_phase_stats(self._h, ctypes.byref(pr), ctypes.byref(rk),
+                                                       ctypes.byref(pv)))
+        return {"completed": c.value, "batches": b.value, "busy_ms": ms.value,
+                "prep_ms": pr.value, "rank_ms": rk.value, "pvalue_ms": pv.value}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -140,14 +144,16 @@ def random_query(rng, n_rows, ref_range=(1_000, 50_000), targets_range=(1, 200),
 
 
 def poisson_run(server: Server, matrix_ids, n_rows_of, rate_qps: float, n_queries: int,
-                seed: int = 0, options=None):
-    """Submits n_queries at Poisson arrival times (rate_qps) over random matrices; waits for
-    all; returns latency percentiles (ms), throughput (tests/s), and the queries' tests."""
+                seed: int = 0, options=None, weights=None):
+    """Submits n_queries at Poisson arrival times (rate_qps) over random matrices (chosen with
+    `weights`, uniformly by default); waits for all; returns latency percentiles (ms, overall
+    and per matrix), throughput (tests/s), and the server's phase times."""
     options = options or dict(zero_handling="min", use_continuity=True, tie_correction=True)
     rng = np.random.default_rng(seed)
+    p = None if weights is None else np.asarray(weights, dtype=float) / np.sum(weights)
     plan = []
     for _ in range(n_queries):
-        mid = int(rng.choice(matrix_ids))
+        mid = int(rng.choice(matrix_ids, p=p))
         gid, T = random_query(rng, n_rows_of[mid])
         plan.append((mid, gid, T))
     gaps = rng.exponential(1.0 / rate_qps, size=n_queries)
@@ -170,7 +176,13 @@ def poisson_run(server: Server, matrix_ids, n_rows_of, rate_qps: float, n_querie
         lat.append(q.latency_ms)
     wall = time.perf_counter() - t0
     lat = np.asarray(lat)
+    mids = np.asarray([mid for mid, _, _ in plan])
+    per_matrix = {}
+    for mid in sorted(set(mids.tolist())):
+        x = lat[mids == mid]
+        per_matrix[int(mid)] = {"queries": int(x.size), "p50_ms": float(np.percentile(x, 50)),
+                                "p99_ms": float(np.percentile(x, 99))}
     return {"rate_qps": rate_qps, "queries": n_queries, "tests": tests,
             "tests_per_s": tests / wall, "wall_s": wall,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(lat.mean()), **server.stats()}
+            "mean_ms": float(lat.mean()), "per_matrix": per_matrix, **server.stats()}

@@ -237,3 +237,38 @@ WORKLOADS = {
     "perturb_screen": perturb_screen,
     "exact_small": exact_small,
 }
+
+
+def resident_atlas(seed: int = 13, n_rows: int = 1_000_000, n_cols: int = 20_000,
+                   per_col: int = 50_000):
+    """The serving workload's largest matrix, generated on the GPU (host generation of 1e9
+    entries would take minutes) and made resident: (log1p-CP10k float32 matrix, integer-count
+    twin), both ResidentMatrix. Every gene stores per_col cells (5 % density at the defaults):
+    row i*s + jitter, s = n_rows // per_col, jitter uniform in [0, s), so rows ascend and never
+    repeat. Counts are 1 + NB(size 2, mean mu_g), mu_g ~ LogNormal(-1, 1.5) clipped to [0.01, 50]
+    (a gamma-Poisson mixture); the float matrix holds log1p(count / library size * 1e4) of each
+    cell, the twin the counts themselves. torch does the generation (device memory plumbing)."""
+    import torch
+    from .resident import ResidentMatrix
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(seed)
+    stride = n_rows // per_col
+    rows = (torch.arange(per_col, device=dev, dtype=torch.int32) * stride)[None, :] + \
+        torch.randint(0, stride, (n_cols, per_col), device=dev, generator=g, dtype=torch.int32)
+    rows = rows.reshape(-1)
+    mu = torch.exp(torch.randn(n_cols, device=dev, generator=g) * 1.5 - 1.0).clamp_(0.01, 50.0)
+    shape = torch.full((n_cols, per_col), 2.0, device=dev)
+    lam = torch._standard_gamma(shape, generator=g) * (mu[:, None] / 2.0)
+    del shape
+    counts = (torch.poisson(lam, generator=g) + 1.0).reshape(-1)
+    del lam
+    lib = torch.zeros(n_rows, device=dev, dtype=torch.float32).index_add_(0, rows.long(), counts)
+    lib.clamp_(min=1.0)
+    values = torch.log1p(counts * (1e4 / lib[rows.long()]))
+    torch.cuda.synchronize()
+    indptr = np.arange(n_cols + 1, dtype=np.int64) * per_col
+    M = ResidentMatrix.from_device(values.data_ptr(), rows.data_ptr(), indptr, n_rows, np.float32)
+    Mi = ResidentMatrix.from_device(counts.data_ptr(), rows.data_ptr(), indptr, n_rows, np.float32)
+    del values, counts, rows, lib
+    torch.cuda.empty_cache()
+    return M, Mi

@@ -187,6 +187,12 @@ int hpdex_matrix_create_csr_idx32(int32_t dtype, const void* data, const int32_t
  * hpdex_group_mean (reference group_mean_core, include_zeros as there). */
 int hpdex_matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_groups,
                             int32_t include_zeros, double* out);
+/* A resident matrix from data already on the device: values (dtype) and int32 row ids are
+ * device pointers (copied into the library's own buffers; the caller keeps ownership), the
+ * n_cols + 1 column pointers are host memory. Otherwise as hpdex_matrix_create_idx32. */
+int hpdex_matrix_create_device(int32_t dtype, const void* d_data, const int32_t* d_rows,
+                               const int64_t* indptr, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                               hpdex_matrix** out);
 int hpdex_matrix_destroy(hpdex_matrix* m);
 int hpdex_matrix_info(const hpdex_matrix* m, int64_t* n_rows, int64_t* n_cols, int64_t* nnz,
                       int64_t* device_bytes);
@@ -307,6 +313,10 @@ int hpdex_server_wait(hpdex_server* s, int64_t query_id, double timeout_s, doubl
 /* completed queries, launches (batches) and summed GPU busy time (ms) since creation */
 int hpdex_server_stats(const hpdex_server* s, int64_t* completed, int64_t* batches,
                        double* busy_ms);
+/* Where a server's time went, summed over its batches: host time preparing and queueing them
+ * (prep_ms: group-id copies, task tables, launches), device time of the rank launches and of
+ * the p-value launches (one per batch), in ms. */
+int hpdex_server_phase_stats(const hpdex_server* s, double* prep_ms, double* rank_ms, double* pvalue_ms);
 /* finishes the admitted work, fails queries still pending, joins the worker */
 int hpdex_server_destroy(hpdex_server* s);
 

@@ -96,3 +96,45 @@ def test_tiny_budget_runs_queries_one_at_a_time():
     for (U1a, Pa), (U1, P) in zip(ref, res):
         np.testing.assert_array_equal(U1a, U1)
         np.testing.assert_array_equal(Pa, P)
+
+
+def test_phase_stats_account_for_the_device_time():
+    """The server's per-phase device times (rank launches, one p-value launch per batch) add up
+    to its busy time; host preparation time is reported beside them."""
+    from hpdex_gb300.serving import Server
+    mats = _matrices()
+    queries = _queries(mats, 12, seed=9)
+    with Server(workspace_bytes=8 << 30, max_batch=16) as srv:
+        ids = [srv.add_matrix(m) for _, m in mats]
+        for q in [srv.submit(ids[mid], gid, T, **o) for mid, gid, T, o in queries]:
+            q.result()
+        st = srv.stats()
+    assert st["completed"] == len(queries)
+    assert st["rank_ms"] > 0.0 and st["pvalue_ms"] >= 0.0 and st["prep_ms"] > 0.0
+    assert abs(st["rank_ms"] + st["pvalue_ms"] - st["busy_ms"]) <= 1e-3 * st["busy_ms"] + 1e-3
+
+
+def test_matrix_from_device_pointers_equals_host_upload():
+    """hpdex_matrix_create_device (values and int32 row ids already in device memory) gives the
+    resident matrix the host upload gives: the same plan results, bit for bit."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch sees no CUDA device")
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.resident import ResidentMatrix
+    w = synthetic.perturb_screen(seed=44, n_rows=12_000, n_cols=200, n_targets=9, ref_size=1_500)
+    d = torch.from_numpy(w.data).cuda()
+    r = torch.from_numpy(w.indices.astype(np.int32)).cuda()
+    torch.cuda.synchronize()
+    Md = ResidentMatrix.from_device(d.data_ptr(), r.data_ptr(), w.indptr, w.n_rows, np.float32)
+    del d, r
+    Mh = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    out = []
+    for M in (Md, Mh):
+        p = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        p.run()
+        out.append(p.download())
+        p.close()
+        M.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
