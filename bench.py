@@ -364,9 +364,26 @@ def serving_leg(M, w, queries=120, rates=(40.0, 2000.0)):
                                       "rank": r["rank_ms"] - base["rank_ms"],
                                       "pvalue": r["pvalue_ms"] - base["pvalue_ms"]},
                          "per_matrix": {names[k]: v for k, v in r["per_matrix"].items()}})
+    # small queries only (the two 50k x 2k matrices), where one launch per query leaves SMs
+    # idle and coalescing several queries into one launch can pay
+    small = []
+    for mode, mb in (("coalesced", 16), ("per_query", 1)):
+        with Server(workspace_bytes=64 << 30, max_batch=mb) as srv:
+            ids = [srv.add_matrix(m) for m in mats[1:3]]
+            srows = {ids[0]: b.n_rows, ids[1]: c.n_rows}
+            poisson_run(srv, ids, srows, rate_qps=5000.0, n_queries=20, seed=3, weights=[0.7, 0.3])
+            base = srv.stats()
+            r = poisson_run(srv, ids, srows, rate_qps=5000.0, n_queries=400, seed=4, weights=[0.7, 0.3])
+        small.append({"mode": mode, "max_batch": mb, "rate_qps": 5000.0, "p50_ms": r["p50_ms"],
+                      "p99_ms": r["p99_ms"], "tests_per_s": r["tests_per_s"],
+                      "launches": r["batches"] - base["batches"],
+                      "phase_ms": {"host_prep": r["prep_ms"] - base["prep_ms"],
+                                   "rank": r["rank_ms"] - base["rank_ms"],
+                                   "pvalue": r["pvalue_ms"] - base["pvalue_ms"]}})
     atlas.close()
     atlas_counts.close()
     return {"matrices": names, "atlas_nnz": 1_000_000_000, "atlas_generation_s": t_gen,
+            "small_queries_saturated": small,
             "query_mix": "70 % float / 30 % integer counts", "queries_per_run": queries,
             "arrival": "Poisson", "rates": {"sustained_qps": rates[0], "saturating_qps": rates[1]},
             "runs": runs,

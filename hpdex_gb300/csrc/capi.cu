@@ -592,6 +592,15 @@ int upload_matrix(hpdex_matrix* m, const void* data, const int64_t* indices, con
     return HPDEX_OK;
 }
 
+// Whether a grouping leaves enough rows out (more than 15 %) for the rank kernel to keep only
+// the stored entries in its decoded copy: the slab passes then re-read fewer entries, for the
+// cost of one warp-wide atomic per 128 entries in the decoding pass.
+int32_t compact_decode(const std::vector<long long>& group_rows, long long n_rows) {
+    long long assigned = 0;
+    for (long long r : group_rows) assigned += r;
+    return (n_rows > 0 && assigned * 100 < n_rows * 85) ? 1 : 0;
+}
+
 // The rank-kernel task of a plan: its matrix, grouping and output buffers.
 RankTask task_of(const hpdex_matrix* m, const hpdex_plan* p) {
     RankTask t{};
@@ -617,6 +626,7 @@ RankTask task_of(const hpdex_matrix* m, const hpdex_plan* p) {
     t.fast_norm = p->opt.fast_norm;
     t.cc = p->opt.use_continuity ? 0.5 : 0.0;
     t.pconst = p->d_pconst.p;
+    t.compact_decode = compact_decode(p->group_rows, m->n_rows);
     return t;
 }
 
@@ -724,6 +734,7 @@ int configure_rank(hpdex_plan* p) {
     a.queue = p->queue.p;
     a.single_gene = -1;
     a.no_histogram = (p->hist_on && m->has_int_cols) ? 0 : 1;
+    a.any_compact = t.compact_decode;
     set_layout_args(a, r, G, p->dk.p, p->dg.p, p->ek.p, p->eg.p, p->acc.p, p->cnt.p);
     return HPDEX_OK;
 }
@@ -2107,6 +2118,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         t.n1 = q->n1.p;
         t.n2 = q->n2.p;
         t.err = q->err.p;
+        t.compact_decode = compact_decode(q->group_rows, R);
     }
     // one work queue over every (query, gene) item of the batch, longest first by nnz class
     std::vector<int32_t> order;
@@ -2166,6 +2178,7 @@ int server_launch(hpdex_server* S, ServerBatch& b) {
         bool any_int = false;  // the histogram variant when a query's matrix may hold integers
         for (auto* q : b.q) any_int = any_int || S->mats[(size_t)q->matrix]->has_int_cols;
         a.no_histogram = any_int ? 0 : 1;
+        for (const RankTask& t : tasks) a.any_compact |= t.compact_decode;
         set_layout_args(a, r, GL, b.dk.p, b.dg.p, b.ek.p, b.eg.p, b.acc.p, b.cnt.p);
         TRY(rank_status(rank_launch(dtype, a, r.grid, r.smem, st), "rank kernel launch"));
     }

@@ -88,6 +88,8 @@ struct RankTask {
     int32_t fast_norm;
     double cc;                 // continuity correction (0.5 or 0)
     const PConst* pconst;      // zero_handling min / max / mix: per target (or null)
+    int32_t compact_decode;    // 1: the decoded copy keeps stored entries only (set when the
+                               // grouping leaves many rows out: fewer entries to re-read)
 };
 
 struct RankArgs {
@@ -120,6 +122,8 @@ struct RankArgs {
     int32_t no_histogram;      // 1: every gene takes the bucket path, and the launch uses the
                                // kernel without the histogram path; 0: the histogram path is
                                // chosen per gene (hist_choice)
+    int32_t any_compact;       // some task has compact_decode set (the launch uses the kernel
+                               // variant that can compact)
     int32_t cta_base;          // per-CTA scratch slice of CTA b: cta_base + b (the plain form
                                // runs one-CTA launches on concurrent streams, each on its slice)
 };
@@ -1004,13 +1008,16 @@ __device__ __forceinline__ void finalize_gene(const RankTask* tk, int c, int G, 
 
 // HIST: the variant with the histogram path (launched when some column of the launch's tasks
 // can hold small integers; without it the bucket path keeps its register allocation).
-template <class V, int NT, bool ACC_SMEM, bool HIST>
+// CPX: the variant that can compact its decoded copy (launched when a task of the launch asks
+// for it, RankTask::compact_decode).
+template <class V, int NT, bool ACC_SMEM, bool HIST, bool CPX>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_gene, s_task;
     __shared__ unsigned long long s_tref;
     __shared__ uint32_t s_maxb, s_slab_hi, s_chunk, s_nbig, s_bigi, s_wdone;
+    __shared__ uint32_t s_ndec;  // entries of the compacted decoded copy
     __shared__ int s_pv_gene, s_pv_task;  // gene whose p-values are pending (-1: none)
     __shared__ uint32_t s_pvq;            // its p-value tiles taken so far
     // the next gene and its column metadata, fetched during the current gene's finalize by a
@@ -1115,6 +1122,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             s_task = s_next_task;
             s_tref = 0ull;
             s_maxb = 0u;
+            s_ndec = 0u;
         }
         for (int g = tid; g < GL; g += NT) { A[g] = 0ull; B[g] = 0ull; nz[g] = 0u; ng[g] = 0u; }
         __syncthreads();
@@ -1179,8 +1187,9 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
         // ---- pass 1 (HBM): decode to (key, group), histograms, per-group counts ----
         uint32_t nref_local = 0;
         // (instantiated for each bucket map, chosen once per gene)
-        auto pass1 = [&](auto vm_tag) {
+        auto pass1 = [&](auto vm_tag, auto cp_tag) {
             constexpr bool VM = decltype(vm_tag)::value;
+            constexpr bool CP = decltype(cp_tag)::value;  // compacted decoded copy
             BucketMap<V> bmap;
             if constexpr (VM) bmap.setup(kmin, kmax, nbl);
             else { bmap.base = kmin; bmap.shift = shift; }
@@ -1210,6 +1219,21 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
                         gl[k] = (uint32_t)r[k] < nrows ? (uint32_t)__ldg(gidp + r[k]) : kNoGroup;
+                    // compacted copy: the warp's stored entries of these 4 rounds take
+                    // consecutive positions (one atomic per warp)
+                    uint32_t cpos = 0;
+                    unsigned okm[4];
+                    if constexpr (CP) {
+                        uint32_t tot = 0;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            okm[k] = __ballot_sync(0xffffffffu, gl[k] != kNoGroup && Val<V>::finite(v[k]) &&
+                                                                    (zh == ZH_NONE || !Val<V>::zero(v[k])));
+                            tot += __popc(okm[k]);
+                        }
+                        if (lane == 0 && tot) cpos = atomicAdd(&s_ndec, tot);
+                        cpos = __shfl_sync(0xffffffffu, cpos, 0);
+                    }
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         const uint32_t i = t + 32u * k + lane;
@@ -1217,7 +1241,16 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                                         (zh == ZH_NONE || !Val<V>::zero(v[k]));
                         const K key = ok ? Val<V>::key(v[k]) : K(0);
                         const uint32_t g = ok ? gl[k] : kNoGroup;
-                        if (i < nraw) { dk[i] = key; dg[i] = (GT)g; }
+                        if constexpr (CP) {
+                            if (ok) {
+                                const uint32_t q = cpos + __popc(okm[k] & ((1u << lane) - 1u));
+                                dk[q] = key;
+                                dg[q] = (GT)g;
+                            }
+                            cpos += __popc(okm[k]);
+                        } else {
+                            if (i < nraw) { dk[i] = key; dg[i] = (GT)g; }
+                        }
                         if (ok) {
                             if (g) red_add<ACC_SMEM>(&nz[g], 1u);
                             else ++nref_local;
@@ -1234,13 +1267,25 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 }
             }
         };
-        if (vmap) pass1(std::true_type{});
-        else pass1(std::false_type{});
+        const bool cdec = CPX && tk->compact_decode != 0;
+        if constexpr (CPX) {
+            if (vmap) {
+                if (cdec) pass1(std::true_type{}, std::true_type{});
+                else pass1(std::true_type{}, std::false_type{});
+            } else {
+                if (cdec) pass1(std::false_type{}, std::true_type{});
+                else pass1(std::false_type{}, std::false_type{});
+            }
+        } else {
+            if (vmap) pass1(std::true_type{}, std::false_type{});
+            else pass1(std::false_type{}, std::false_type{});
+        }
         nref_local = __reduce_add_sync(0xffffffffu, nref_local);
         if (lane == 0 && nref_local) red_add<ACC_SMEM>(&nz[0], nref_local);
         __syncthreads();
         block_scan2<NT>(hall, href, NB, s_wsx, s_wsy, &s_maxb);
         const uint32_t n = hall[NB];
+        const uint32_t ndec = cdec ? s_ndec : nraw;  // entries of the decoded copy
         // 16-bit key offsets inside a bucket: the buckets of the key map hold keys that differ
         // in their low `shift` bits only
         const bool compact = !vmap && shift <= 16;
@@ -1291,25 +1336,25 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
                 else { bmap.base = kmin; bmap.shift = shift; }
                 const bool all = nslabs == 1u;
                 uint32_t t = 128u * (uint32_t)warp;
-                if (t < nraw) {
+                if (t < ndec) {
                     K k4[4];
                     uint32_t g4[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         const uint32_t i = t + 32u * k + lane;
-                        k4[k] = i < nraw ? dk[i] : K(0);
-                        g4[k] = i < nraw ? (uint32_t)dg[i] : kNoGroup;
+                        k4[k] = i < ndec ? dk[i] : K(0);
+                        g4[k] = i < ndec ? (uint32_t)dg[i] : kNoGroup;
                     }
                     for (;;) {
                         const uint32_t tn = t + 4u * NT;
-                        const bool more = tn < nraw;
+                        const bool more = tn < ndec;
                         K kn[4];
                         uint32_t gn[4];
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
                             const uint32_t i = tn + 32u * k + lane;
-                            kn[k] = (more && i < nraw) ? dk[i] : K(0);
-                            gn[k] = (more && i < nraw) ? (uint32_t)dg[i] : kNoGroup;
+                            kn[k] = (more && i < ndec) ? dk[i] : K(0);
+                            gn[k] = (more && i < ndec) ? (uint32_t)dg[i] : kNoGroup;
                         }
                         uint32_t bb[4];
                         bool in[4];
@@ -1343,8 +1388,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
             __syncthreads();
             if (slab + 1u == nslabs) {
                 // the decoded copy is dead: drop its lines from L2 instead of writing them back
-                l2_discard<NT>(dk, (size_t)nraw * sizeof(K));
-                l2_discard<NT>(dg, (size_t)nraw * sizeof(GT));
+                l2_discard<NT>(dk, (size_t)ndec * sizeof(K));
+                l2_discard<NT>(dg, (size_t)ndec * sizeof(GT));
             }
 
             // ---- rank ----

@@ -9,21 +9,24 @@ namespace hpdex {
 
 cudaError_t HPDEX_CAT(rank_launch_, HPDEX_RANK_T)(const RankArgs& a, int grid, size_t smem,
                                                   cudaStream_t s) {
-    auto k = !a.acc_in_smem   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>
-             : a.no_histogram ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false>
-                              : mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>;
+    auto k = !a.acc_in_smem   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>
+             : !a.no_histogram ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>
+             : a.any_compact   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true>
+                               : mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false>;
     k<<<grid, 1024, smem, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t HPDEX_CAT(rank_occupancy_, HPDEX_RANK_T)(size_t smem, size_t smem_optin,
                                                      int acc_in_smem, int* blocks) {
-    // both variants of an accumulator layout get the same shared-memory limit
-    decltype(&mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>) ks[2] = {
-        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false>
-                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>,
-        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true>
-                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false>};
+    // the variants of an accumulator layout get the same shared-memory limit
+    decltype(&mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>) ks[3] = {
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>};
     for (auto k : ks) {
         cudaFuncAttributes fa;
         cudaError_t e = cudaFuncGetAttributes(&fa, k);
