@@ -1466,7 +1466,7 @@ int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits) {
         configure_rank(p);
     }
     p->ra.erfc_table = keep.erfc_table;
-    p->ra.no_drain_wait = keep.no_drain_wait;
+    p->ra.drain_wait = keep.drain_wait;
     p->ra.no_histogram = keep.no_histogram;
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
     if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
@@ -1486,9 +1486,9 @@ int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on) {
 
 int hpdex_plan_set_drain_wait(hpdex_plan* p, int32_t on) {
     if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
-    const int32_t off = on ? 0 : 1;
-    if (p->ra.no_drain_wait == off) return HPDEX_OK;
-    p->ra.no_drain_wait = off;
+    const int32_t w = on ? 1 : 0;
+    if (p->ra.drain_wait == w) return HPDEX_OK;
+    p->ra.drain_wait = w;
     if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
     if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
     return HPDEX_OK;

@@ -117,8 +117,9 @@ struct RankArgs {
     int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
     const double* erfc_table;  // non-null: the kernel also computes the asymptotic p-values
                                // (P replaces the tie sums); null: a p-value kernel follows
-    int32_t no_drain_wait;     // 1: a warp that finds a big-list entry not yet published gives
-                               // up at once (diagnostic: the results must not change)
+    int32_t drain_wait;        // 1: a warp that finds a big-list entry not yet published polls
+                               // for it a bounded number of times; 0 (the default): it goes to
+                               // the block barrier at once (the results are the same)
     int32_t no_histogram;      // 1: every gene takes the bucket path, and the launch uses the
                                // kernel without the histogram path; 0: the histogram path is
                                // chosen per gene (hist_choice)
@@ -371,9 +372,12 @@ __device__ __forceinline__ void add_pair(const Acc& acc, uint32_t g, unsigned lo
 // the target elements with the same key and group (keys of different buckets are never
 // compared: they may be 16-bit offsets inside their buckets). Summed over a run of c0 reference and
 // s target-g elements these give s*(2*lref + c0), (c0+s)^3-(c0+s)-(c0^3-c0) and c0^3-c0.
-// lt and c0 come from broadcasting the (few) reference lanes; s from the warp's group
-// counters, which show which groups occur more than once in the round, and a pairwise
-// comparison among those lanes only. `cnt` is zero on entry and on exit.
+// Most buckets of a round hold one key (a tie run): there every reference element of the
+// bucket is equal (lt = 0, c0 = its reference lanes) and equal groups mean equal (key, group).
+// Buckets with more than one key take lt and c0 from broadcasting their (few) reference lanes.
+// s: the warp's group counters show which groups occur more than once in the round; such lanes
+// of one-key buckets match their group, those of other buckets compare pairwise among
+// themselves. `cnt` is zero on entry and on exit.
 template <class K, bool SH>
 __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, unsigned sub,
                                               uint32_t rb, const Acc& acc, uint32_t* cnt,
@@ -383,8 +387,14 @@ __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, un
     const bool is_ref = active && g == 0u;
     const bool is_tar = active && g != 0u;
     const unsigned refm = __ballot_sync(0xffffffffu, is_ref);
-    uint32_t lt = 0, c0 = 0;
-    for (unsigned r = refm; r; r &= r - 1u) {
+    // buckets with more than one key: some lane's key differs from its bucket's first lane's
+    const int first = active ? __ffs((int)sub) - 1 : (int)(threadIdx.x & 31);
+    const K kf = __shfl_sync(0xffffffffu, key, first);
+    const unsigned diff = __ballot_sync(0xffffffffu, active && key != kf);
+    const bool mixed = (sub & diff) != 0u;
+    const unsigned mixm = __ballot_sync(0xffffffffu, active && mixed);
+    uint32_t lt = 0, c0 = mixed ? 0u : (uint32_t)__popc(refm & sub);
+    for (unsigned r = refm & mixm; r; r &= r - 1u) {
         const int j = __ffs((int)r) - 1;
         const K kj = __shfl_sync(0xffffffffu, key, j);
         if ((sub >> j) & 1u) {
@@ -404,14 +414,21 @@ __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, un
     const unsigned rep = __ballot_sync(0xffffffffu, ng > 1u);
     uint32_t s = 1;
     if (rep) {
-        uint32_t c = 0;
-        for (unsigned r = rep; r; r &= r - 1u) {
-            const int j = __ffs((int)r) - 1;
-            const K kj = __shfl_sync(0xffffffffu, key, j);
-            const uint32_t gj = __shfl_sync(0xffffffffu, g, j);
-            c += ((sub >> j) & 1u) && gj == g && kj == key;  // same bucket: keys may be offsets
+        // every lane of a one-key bucket whose group repeats in the round is in `one`, so the
+        // match over `one` sees all lanes of its bucket with its group
+        const unsigned one = __ballot_sync(0xffffffffu, ng > 1u && !mixed);
+        if (ng > 1u && !mixed) s = (uint32_t)__popc(__match_any_sync(one, g) & sub);
+        const unsigned many = rep & ~one;
+        if (many) {
+            uint32_t c = 0;
+            for (unsigned r = many; r; r &= r - 1u) {
+                const int j = __ffs((int)r) - 1;
+                const K kj = __shfl_sync(0xffffffffu, key, j);
+                const uint32_t gj = __shfl_sync(0xffffffffu, g, j);
+                c += ((sub >> j) & 1u) && gj == g && kj == key;  // same bucket: keys may be offsets
+            }
+            if (ng > 1u && mixed) s = c;
         }
-        if (ng > 1u) s = c;
     }
     __syncwarp();
     if (is_tar) {
@@ -681,10 +698,12 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
     }
     // Big buckets: a warp whose chunks are done takes listed buckets while other warps may
     // still be listing (no barrier between the phases). An entry is published by its slot
-    // (s_nbig) and then its bucket id; a taker waits a bounded time for the id and marks the
-    // entry taken. When every warp has finished its chunks and the taker's index is past the
-    // final count, the list is exhausted. A wait that runs out leaves its entry for the
-    // pass after the barrier, which resolves every entry not marked taken.
+    // (s_nbig) and then its bucket id; a taker that finds the id marks the entry taken. A taker
+    // that finds it not yet published goes to the barrier (by default: on the screen and exact
+    // workloads that is 1% and 7% faster than waiting) or, with `wait_polls`, polls for it a
+    // bounded number of times. When every warp has finished its chunks and the taker's index is
+    // past the final count, the list is exhausted. The pass after the barrier resolves every
+    // entry not marked taken.
     __threadfence_block();
     __syncwarp();
     if (lane == 0) atomicAdd(s_wdone, 1u);
@@ -1031,7 +1050,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     __shared__ uint8_t s_tbl[NT / 32][32];  // per warp: packable bucket -> lane (rank rounds)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wait_polls = a.no_drain_wait ? 0 : kDrainWaitIters;
+    const int wait_polls = a.drain_wait ? kDrainWaitIters : 0;
     const int GL = a.G;  // layout G
     const int NBMAX = 1 << a.nb_max_log2;
     const RankSmem L(a.nb_max_log2, GL, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,

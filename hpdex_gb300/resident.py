@@ -170,8 +170,9 @@ class Plan:
         _lib.check(_lib.lib().hpdex_plan_set_histogram(self._h, int(bool(on))))
 
     def set_drain_wait(self, on: bool) -> None:
-        """Diagnostic: off makes the rank kernel's bounded waits for large buckets give up at
-        once, so the pass after the block barrier resolves them; results do not change."""
+        """Diagnostic: on makes a warp of the rank kernel wait a bounded number of polls for a
+        large bucket another warp is still listing (off, the default, leaves it to the pass after
+        the block barrier); results do not change."""
         _lib.check(_lib.lib().hpdex_plan_set_drain_wait(self._h, int(bool(on))))
 
     def download(self):

@@ -232,10 +232,10 @@ int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits);
 int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on);
 
 /* Diagnostic. The rank kernel lets a warp resolve a large bucket while other warps of its CTA
- * are still listing them; it waits a bounded number of polls for an entry to be published and,
- * when they run out, leaves the entry to a pass after the next block barrier. on = 0 makes
- * every such wait give up at once, so the fallback pass does all of that work; the results
- * must not change (on = 1, the default, restores the bounded wait). */
+ * are still listing them. By default (on = 0) a warp that finds the next list entry not yet
+ * published leaves it to a pass after the next block barrier; on = 1 makes it wait for the entry
+ * a bounded number of polls first (slower on the measured workloads). The results are the same
+ * either way. */
 int hpdex_plan_set_drain_wait(hpdex_plan* p, int32_t on);
 
 /* Device times (ms, CUDA events on the launching stream) of the last hpdex_plan_run:

@@ -94,9 +94,9 @@ def test_large_columns_many_targets():
 
 @pytest.mark.parametrize("fused", [True, False])
 def test_drain_wait_fallback_gives_identical_results(fused):
-    """Warps that resolve listed big buckets while other warps still list them wait a bounded
-    number of polls for an entry; with no polls at all every such entry goes to the pass after
-    the block barrier. Both must give the same doubles, in both p-value forms."""
+    """Warps that resolve listed big buckets while other warps still list them either leave an
+    entry not yet published to the pass after the block barrier (the default) or wait a bounded
+    number of polls for it. Both must give the same doubles, in both p-value forms."""
     from hpdex_gb300.resident import BATCHED, ResidentMatrix
     sizes = [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]
     w = _workload(3, 150_000, COLUMNS, 30_000, sizes)
@@ -106,7 +106,7 @@ def test_drain_wait_fallback_gives_identical_results(fused):
         plan.set_fused_pvalues(fused)
         plan.run(BATCHED)
         U1a, Pa = plan.download()
-        plan.set_drain_wait(False)
+        plan.set_drain_wait(True)
         for _ in range(2):
             plan.run(BATCHED)
             U1b, Pb = plan.download()
