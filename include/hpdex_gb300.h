@@ -270,8 +270,7 @@ int hpdex_plan_timings(const hpdex_plan* p, float* ms3, int32_t* launches);
  * taken in column order (no longest-first scheduling).
  *
  * The first call on a device does a one-time set-up (it resolves the device address of
- * the array with cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call shares the one array and finds the previous call's contents in it: calls
+ * the array with cudaGetSymbolAddress). Every call shares the one array and finds the previous call's contents in it: calls
  * that overlap on the GPU (two host threads, or two streams) race and corrupt each other,
  * so serialise them.
  */
