@@ -179,6 +179,56 @@ __global__ void __launch_bounds__(1024) upload_chunk_kernel(const V* __restrict_
     }
 }
 
+// The same upload with 16-byte accesses: four consecutive entries per thread and step (values and
+// row ids as one or two 16-byte words). Host reads over the link reach about 205 GB/s this way
+// against 180 GB/s with element-wide loads (GB300, pageable memory; 212 GB/s is the page-locked
+// copy rate). Entries [0, lead) and the last (n - lead) % 4 are copied one by one; from `lead`
+// on, all four arrays are aligned to their quads (the launcher checks).
+template <int B> struct Quad;  // four elements of B bytes
+template <> struct Quad<1> { using T = uint32_t; };
+template <> struct Quad<2> { using T = uint2; };
+template <> struct Quad<4> { using T = uint4; };
+template <> struct Quad<8> { struct __align__(16) T { ulonglong2 a, b; }; };
+
+template <class V, class R>
+__global__ void __launch_bounds__(1024) upload_chunk_quad_kernel(const V* __restrict__ hv, const R* __restrict__ hr,
+                                                                 V* __restrict__ dv, int32_t* __restrict__ dr,
+                                                                 long long n, long long n_rows, int lead) {
+    using QV = typename Quad<sizeof(V)>::T;
+    using QR = typename Quad<sizeof(R)>::T;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    auto narrow = [&](long long r) { return (r >= 0 && r < n_rows) ? (int32_t)r : -1; };
+    const long long nq = (n - lead) / 4;
+    const long long tail = lead + 4 * nq;
+    if (tid < lead) { dv[tid] = hv[tid]; dr[tid] = narrow((long long)hr[tid]); }
+    if (tail + tid < n) { dv[tail + tid] = hv[tail + tid]; dr[tail + tid] = narrow((long long)hr[tail + tid]); }
+    const QV* qv = reinterpret_cast<const QV*>(hv + lead);
+    const QR* qr = reinterpret_cast<const QR*>(hr + lead);
+    QV* ov = reinterpret_cast<QV*>(dv + lead);
+    int4* orow = reinterpret_cast<int4*>(dr + lead);
+    auto rows4 = [&](const QR& w) {
+        if constexpr (sizeof(R) == 4)
+            return make_int4(narrow((int32_t)w.x), narrow((int32_t)w.y), narrow((int32_t)w.z), narrow((int32_t)w.w));
+        else
+            return make_int4(narrow((long long)w.a.x), narrow((long long)w.a.y), narrow((long long)w.b.x),
+                             narrow((long long)w.b.y));
+    };
+    long long q = tid;
+    for (; q + stride < nq; q += 2 * stride) {  // two quads in flight per thread
+        const QV v0 = qv[q], v1 = qv[q + stride];
+        const QR r0 = qr[q], r1 = qr[q + stride];
+        ov[q] = v0;
+        ov[q + stride] = v1;
+        orow[q] = rows4(r0);
+        orow[q + stride] = rows4(r1);
+    }
+    if (q < nq) {
+        ov[q] = qv[q];
+        orow[q] = rows4(qr[q]);
+    }
+}
+
 // Device memory cache. A released block stays reserved for its device and is handed out
 // again to a request of at most its size and at least half of it, so repeated calls (the
 // one-shot call allocates a matrix, a plan and their scratch every time) skip cudaMalloc and
@@ -481,7 +531,24 @@ struct UploadLaunch {  // one chunk, straight from the host arrays (see upload_c
     static int run(const void* hv, const int64_t* hr64, const int32_t* hr32, void* dv, int32_t* dr,
                    long long n, long long n_rows, cudaStream_t s) {
         if (n == 0) return HPDEX_OK;
-        if (hr32)
+        // quads from the first entry whose device row id is 16-byte aligned, when the other
+        // three arrays are aligned to their quads there too (numpy's arrays are, at any chunk
+        // start that is a multiple of 4 entries away)
+        const int lead = (int)((4 - ((uintptr_t)dr / 4) % 4) % 4);
+        auto aligned = [&](const void* p, size_t elem, size_t a) {
+            return ((uintptr_t)p + (size_t)lead * elem) % a == 0;
+        };
+        const size_t qv = std::min<size_t>(16, 4 * sizeof(V));
+        const size_t qr = 16;
+        const bool quad = n >= lead + 4 && aligned(hv, sizeof(V), qv) && aligned(dv, sizeof(V), qv) &&
+                          aligned(hr32 ? (const void*)hr32 : (const void*)hr64, hr32 ? 4 : 8, qr);
+        if (quad && hr32)
+            upload_chunk_quad_kernel<V, int32_t><<<kUploadCTAs, 1024, 0, s>>>(
+                static_cast<const V*>(hv), hr32, static_cast<V*>(dv), dr, n, n_rows, lead);
+        else if (quad)
+            upload_chunk_quad_kernel<V, int64_t><<<kUploadCTAs, 1024, 0, s>>>(
+                static_cast<const V*>(hv), hr64, static_cast<V*>(dv), dr, n, n_rows, lead);
+        else if (hr32)
             upload_chunk_kernel<V, int32_t><<<kUploadCTAs, 1024, 0, s>>>(
                 static_cast<const V*>(hv), hr32, static_cast<V*>(dv), dr, n, n_rows);
         else
@@ -1691,6 +1758,7 @@ int matrix_group_mean(const hpdex_matrix* m, const int32_t* group_id, int64_t n_
 namespace {
 
 constexpr int kPipelineChunks = 12;
+constexpr int kComputeStreams = 2;  // chunks alternate between this many compute streams
 
 // Row ids come as int64 (`indices`, narrowed on the device through staging buffers) or as
 // int32 (`indices32`, uploaded straight into the matrix: half the bytes; ids outside
@@ -1764,17 +1832,25 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     if (!idx32 && !kernel_upload)
         for (auto& b : stage) TRY(b.alloc((size_t)std::max<long long>(max_chunk, 1)));
 
-    struct Res {  // copy stream and events of this call, released once the copy stream drained
-        cudaStream_t copy = nullptr;
+    struct Res {  // copy stream, second compute stream and events of this call, released once
+                  // their streams drained
+        cudaStream_t copy = nullptr, comp2 = nullptr;
         std::vector<cudaEvent_t> ev;
         ~Res() {
             if (copy) cudaStreamSynchronize(copy);
+            if (comp2) cudaStreamSynchronize(comp2);
             for (auto e : ev) if (e) cudaEventDestroy(e);
             if (copy) cudaStreamDestroy(copy);
+            if (comp2) cudaStreamDestroy(comp2);
         }
     } r;
-    CUDA_TRY(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
-    r.ev.assign((size_t)(2 * K), nullptr);
+    // the copy stream at the highest priority: when SMs free up, a pending upload kernel's CTAs
+    // take them before a rank kernel's
+    int prio_least = 0, prio_greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&r.copy, cudaStreamNonBlocking, prio_greatest));
+    CUDA_TRY(cudaStreamCreateWithFlags(&r.comp2, cudaStreamNonBlocking));
+    r.ev.assign((size_t)(2 * K + 3), nullptr);
     for (auto& e : r.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     cudaStream_t sx = r.copy;
     auto enqueue_copy = [&](int j) -> int {  // upload position j: chunk seq[j], staging buffer j & 1
@@ -1831,6 +1907,23 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     p->fused_pvalues = false;
     p->ra.erfc_table = nullptr;
     TRY(first_copy);
+    // Chunks alternate between two compute streams, so that the next chunk's rank kernel takes
+    // the SMs of the previous one's last CTAs as they finish instead of waiting for all of them
+    // (a chunk holds a few genes per CTA, so its tail is long). Chunks on the second stream use
+    // a scratch set of their own.
+    cudaStream_t sc2 = r.comp2;
+    RankLayout lay2;
+    TRY(rank_layout(m->dev, dtype, (int)p->G, m->max_col_nnz, &lay2, p->nbl));
+    DevBuf<unsigned char> dk2, dg2, ek2, eg2, acc2;
+    DevBuf<uint32_t> cnt2;
+    TRY(dk2.alloc(lay2.dk_bytes()));
+    TRY(dg2.alloc(lay2.dg_bytes()));
+    if (lay2.need_slab_scratch) {
+        TRY(ek2.alloc(lay2.dk_bytes()));
+        TRY(eg2.alloc(lay2.dg_bytes()));
+    }
+    if (!lay2.acc_in) TRY(acc2.alloc(lay2.acc_bytes((int)p->G)));
+    TRY(cnt2.alloc(lay2.cnt_words((int)p->G)));
     const long long T = p->T;
     CUDA_TRY(cudaMemcpyAsync(p->order.p, order.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, p->stream));
 
@@ -1864,11 +1957,14 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
         });
     }
     cudaStream_t sc = p->stream;
-    // every exit drains the compute stream before the plan, the toucher flag or the buffers go
+    // every exit drains both compute streams before the plan, the toucher flag or the buffers go
     struct Drain {
-        cudaStream_t s;
-        ~Drain() { cudaStreamSynchronize(s); }
-    } drain{sc};
+        cudaStream_t s, s2;
+        ~Drain() {
+            cudaStreamSynchronize(s);
+            cudaStreamSynchronize(s2);
+        }
+    } drain{sc, sc2};
 
     CUDA_TRY(cudaMemsetAsync(p->err.p, 0xff, kErrWords * sizeof(unsigned long long), sc));
     CUDA_TRY(cudaMemsetAsync(queues.p, 0, sizeof(int32_t) * K, sc));
@@ -1880,28 +1976,37 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
             prepare_group_ids_kernel<uint32_t><<<grid, 256, 0, sc>>>(p->gid.p, n_rows, (int32_t)p->G, reinterpret_cast<uint32_t*>(p->gidc.p));
         CUDA_TRY(cudaGetLastError());
     }
+    cudaEvent_t ev_fork = r.ev[(size_t)(2 * K)], ev_join = r.ev[(size_t)(2 * K + 1)];
+    cudaEvent_t ev_touch = r.ev[(size_t)(2 * K + 2)];
+    CUDA_TRY(cudaEventRecord(ev_fork, sc));
+    CUDA_TRY(cudaStreamWaitEvent(sc2, ev_fork, 0));
     for (int j = 0; j < K; ++j) {
         const int k = seq[(size_t)j];
         const long long c0 = cb[k], c1 = cb[k + 1];
         const long long p0 = indptr[c0], nk = indptr[c1] - p0;
-        CUDA_TRY(cudaStreamWaitEvent(sc, r.ev[2 * j], 0));
+        const bool second = kComputeStreams > 1 && (j & 1) != 0;
+        cudaStream_t sj = second ? sc2 : sc;
+        CUDA_TRY(cudaStreamWaitEvent(sj, r.ev[2 * j], 0));
         if (nk && !idx32 && !kernel_upload) {
-            narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sc>>>(
+            narrow_rows_kernel<<<(int)std::min<long long>((nk + 255) / 256, (long long)m->dev.sms * 16), 256, 0, sj>>>(
                 stage[j & 1].p, m->rows.p + p0, nk, n_rows);
             CUDA_TRY(cudaGetLastError());
         }
-        CUDA_TRY(cudaEventRecord(r.ev[2 * j + 1], sc));
+        CUDA_TRY(cudaEventRecord(r.ev[2 * j + 1], sj));
         TRY(dispatch_dtype<KeyRangeLaunch>(dtype, (const void*)m->data.p, (const int64_t*)(m->indptr.p + c0), c1 - c0,
                                            m->col_kmin.p + c0, m->col_kmax.p + c0, m->col_has_zero.p + c0, nk,
-                                           m->dev.sms, sc));
+                                           m->dev.sms, sj));
         RankArgs ra = p->ra;
         ra.order = p->order.p + c0;
         ra.n_order = (int32_t)(c1 - c0);
         ra.queue = queues.p + k;
         ra.single_gene = -1;
-        // with kernel uploads, kUploadCTAs SMs stay free for the next chunk's upload
-        const int grid = kernel_upload ? std::max(1, p->rank_grid - kUploadCTAs) : p->rank_grid;
-        TRY(rank_status(rank_launch(dtype, ra, grid, p->rank_smem, sc), "rank kernel launch"));
+        if (second)
+            set_layout_args(ra, lay2, (int)p->G, dk2.p, dg2.p, ek2.p, eg2.p, acc2.p, cnt2.p);
+        // with kernel uploads, kUploadCTAs SMs stay free for the next chunk's upload (the last
+        // chunk has none after it)
+        const int grid = kernel_upload && j + 1 < K ? std::max(1, p->rank_grid - kUploadCTAs) : p->rank_grid;
+        TRY(rank_status(rank_launch(dtype, ra, grid, p->rank_smem, sj), "rank kernel launch"));
         PArgs pa{};
         pa.U1 = p->U1.p;
         pa.P = p->P.p;
@@ -1924,14 +2029,19 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
                 const auto* done = static_cast<const std::atomic<int>*>(f);
                 while (!done->load(std::memory_order_acquire)) std::this_thread::yield();
             }, &touched));
+            CUDA_TRY(cudaEventRecord(ev_touch, sc));
         }
+        if (direct && !pinned_out && j == 1)  // the second stream's p-values write those pages too
+            CUDA_TRY(cudaStreamWaitEvent(sc2, ev_touch, 0));
         if (pa.n) {
             const int grid = (int)std::min<long long>((pa.n + 255) / 256, (long long)m->dev.sms * 8);
-            mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, sc>>>(pa);
+            mwu_pvalue_asymptotic_kernel<<<grid, 256, 0, sj>>>(pa);
             CUDA_TRY(cudaGetLastError());
         }
         if (j + 1 < K) TRY(enqueue_copy(j + 1));
     }
+    CUDA_TRY(cudaEventRecord(ev_join, sc2));
+    CUDA_TRY(cudaStreamWaitEvent(sc, ev_join, 0));
     CUDA_TRY(cudaStreamSynchronize(sc));
     TRY(check_device_errors(p.get()));
     if (!direct) TRY(hpdex_plan_download(p.get(), U1_out, P_out));

@@ -121,3 +121,37 @@ def test_int32_row_ids_resident_matrix():
         out.append((*plan.download(), M.group_mean(w.group_id, w.n_targets + 1)))
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.float32, np.float64])
+def test_upload_at_every_alignment(dtype):
+    """The one-shot call reads the caller's arrays in 16-byte words from the first entry of a
+    chunk where host and device arrays are all aligned, element by element before it, after
+    the last whole quad, and everywhere when the host arrays cannot be aligned. Value and row-id
+    arrays placed 0-5 elements into larger buffers (int64 and int32 row ids, ids outside
+    [0, n_rows) among them) give the resident path's results bit for bit."""
+    from hpdex_gb300 import synthetic
+    from hpdex_gb300.backend.bin import kernel
+    w = synthetic.umi_counts(seed=21, n_rows=9_000, n_cols=137, n_targets=11)
+    w.data = w.data.astype(dtype)
+    idx = w.indices.astype(np.int64).copy()
+    idx[::89] = w.n_rows + 3
+    idx[5::97] = -2
+    w.indices = idx
+    U1r, Pr = _resident(w, zero_handling="min", use_continuity=True)
+    nnz = w.data.size
+
+    def placed(a, off):
+        buf = np.zeros(a.size + 8, a.dtype)
+        v = buf[off:off + a.size]
+        v[:] = a
+        return v
+
+    for off_v, off_r in ((0, 0), (1, 0), (0, 1), (2, 3), (4, 2), (5, 5)):
+        for rows in (idx, idx.astype(np.int32)):
+            U1, P = kernel.mannwhitneyu(placed(w.data, off_v), placed(rows, off_r), w.indptr,
+                                        w.group_id, w.n_targets, use_continuity=True,
+                                        zero_handling=1, fast_norm=False)
+            np.testing.assert_array_equal(U1, U1r)
+            np.testing.assert_array_equal(P, Pr)
+    assert nnz > 12 * 4
