@@ -925,15 +925,25 @@ static __device__ __noinline__ unsigned long long hist_gene(
     // the previous gene's p-values: as on the bucket path, some warps start on them
     if (pv_tk && warp < kPvWarps) pvalue_tiles(pv_tk, pv_c, s_pvq, erfc_table);
     __syncthreads();
-    // one streaming pass: each stored element increments its (value, group) counter
+    // one streaming pass: each stored element increments its (value, group) counter; the row
+    // ids and values of the next four elements are in flight while the current ones' group ids
+    // are gathered and counted
+    int32_t r[4];
+    V v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t e = (uint32_t)tid + (uint32_t)(k * NT);
+        r[k] = e < nraw ? __ldcs(rows + e) : -1;
+        v[k] = e < nraw ? ld_stream(data + e) : V(0);
+    }
     for (uint32_t i = (uint32_t)tid; i < nraw; i += 4u * NT) {
-        int32_t r[4];
-        V v[4];
+        int32_t rn[4];
+        V vn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t e = i + (uint32_t)(k * NT);
-            r[k] = e < nraw ? __ldcs(rows + e) : -1;
-            v[k] = e < nraw ? ld_stream(data + e) : V(0);
+            const uint32_t e = i + 4u * NT + (uint32_t)(k * NT);
+            rn[k] = e < nraw ? __ldcs(rows + e) : -1;
+            vn[k] = e < nraw ? ld_stream(data + e) : V(0);
         }
         uint32_t gl[4];
 #pragma unroll
@@ -948,6 +958,8 @@ static __device__ __noinline__ unsigned long long hist_gene(
                 red_add<true>(&hc[(gl[k] ? 4u + gl[k] * (uint32_t)hVp : 0u) + bin], 1u);
             }
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { r[k] = rn[k]; v[k] = vn[k]; }
     }
     __syncthreads();
     block_scan1<NT>(hc, hV, ws);  // hc[v] = reference elements below v, hc[V] = all of them
