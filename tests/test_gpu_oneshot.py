@@ -155,3 +155,28 @@ def test_upload_at_every_alignment(dtype):
             np.testing.assert_array_equal(U1, U1r)
             np.testing.assert_array_equal(P, Pr)
     assert nnz > 12 * 4
+
+
+def test_pageable_output_arrays():
+    """Outputs in ordinary (pageable, never written) numpy arrays: on coherent-memory systems the
+    p-value kernels of both compute streams write them directly, after a host thread has touched
+    their pages; elsewhere the results are copied back. Either way the results equal the
+    wrapper's (page-locked outputs), on a workload of several chunks."""
+    import ctypes
+    from hpdex_gb300 import _lib, synthetic
+    from hpdex_gb300.backend.bin import kernel
+    from hpdex_gb300.resident import make_options
+    w = synthetic.perturb_screen(seed=33, n_rows=40_000, n_cols=900, n_targets=60, ref_size=4_000)
+    U1r, Pr = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
+                                  use_continuity=True, zero_handling=1, fast_norm=False)
+    opt = make_options(tie_correction=True, use_continuity=True, zero_handling="min")
+    for _ in range(2):
+        U1 = np.empty((w.n_targets, w.n_cols))
+        P = np.empty((w.n_targets, w.n_cols))
+        st = _lib.lib().hpdex_mannwhitneyu(
+            _lib.DTYPE_CODES[w.data.dtype.name], w.data.ctypes.data, w.indices.ctypes.data,
+            w.indptr.ctypes.data, w.n_rows, w.n_cols, w.data.size, w.group_id.ctypes.data,
+            w.n_targets, ctypes.byref(opt), -1, U1.ctypes.data, P.ctypes.data)
+        assert st == 0, _lib.lib().hpdex_last_error()
+        np.testing.assert_array_equal(U1, U1r)
+        np.testing.assert_array_equal(P, Pr)
