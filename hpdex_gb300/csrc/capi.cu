@@ -436,6 +436,8 @@ struct hpdex_plan {
     RankArgs ra{};
     bool hist_on = true;         // histogram path allowed (hpdex_plan_set_histogram)
     int nbl = 13;                // bucket table of 2^nbl entries (hpdex_plan_set_bucket_bits)
+    int cnt_mode = -1;           // run counters: -1 automatic, 1 shared, 0 global memory
+                                 // (hpdex_plan_set_run_counters)
     bool fused_pvalues = false;  // asymptotic p-values computed inside the rank kernel
     size_t rank_smem = 0;
     int rank_grid = 0;
@@ -713,7 +715,7 @@ std::vector<PConst> target_consts(const std::vector<long long>& group_rows, int 
 // Shared-memory layout, grid and scratch sizes of a rank launch for value type `dtype`,
 // layout G and longest column `max_col`.
 struct RankLayout {
-    int nbl = 13, tie_warps = kRankThreads / 32, acc_in = 1, cap = 0, grid = 0, kb = 4, gb = 2;
+    int nbl = 13, tie_warps = kRankThreads / 32, acc_in = 1, cnt_in = 1, cap = 0, grid = 0, kb = 4, gb = 2;
     size_t smem = 0;
     long long slice = 0;
     bool need_slab_scratch = false;  // some column exceeds the shared-memory capacity
@@ -723,24 +725,39 @@ struct RankLayout {
     size_t cnt_words(int G) const { return (size_t)grid * tie_warps * ((size_t)RankSmem::cnt_words(G) + G); }
 };
 
+// Run counters (per warp, 16 bits per group) stay in shared memory up to this many groups; above
+// it they take so much of it (64 KB at 1,024 groups) that the elements' room is worth more: on
+// the exact-mode workload (1,501 groups) the counters in global memory, with rounds resolving
+// repeated groups by warp match, took the step from 8.01 to 5.51 ms (slabs of 4,600 elements
+// became slabs of 18,000).
+constexpr int kCountersSharedMaxG = 1024;
+
+// cnt_mode: 1 run counters in shared memory (when the accumulators are), 0 in global memory,
+// -1 automatic (kCountersSharedMaxG).
 int rank_layout(const DeviceInfo& dev, int dtype, int G, long long max_col, RankLayout* out,
-                int nbl = 13) {
+                int nbl = 13, int cnt_mode = -1) {
     RankLayout r;
     r.nbl = nbl;
     r.kb = key_bytes(dtype);
     const size_t budget = std::min(dev.smem_per_sm - dev.smem_reserved, dev.smem_optin) - 2048;
-    // accumulators and run counters live together: both in shared memory, or both global
-    RankSmem L(r.nbl, G, r.tie_warps, 1, 1, 0, r.kb);
-    if (L.total + 16384 > budget) { r.acc_in = 0; L = RankSmem(r.nbl, G, r.tie_warps, 0, 0, 0, r.kb); }
+    // accumulators in shared memory when they fit (with the counters, when those are there too);
+    // else both in global memory
+    r.cnt_in = (cnt_mode == 1 || (cnt_mode < 0 && G <= kCountersSharedMaxG)) ? 1 : 0;
+    RankSmem L(r.nbl, G, r.tie_warps, 1, r.cnt_in, 0, r.kb);
+    if (L.total + 16384 > budget) {
+        r.acc_in = 0;
+        r.cnt_in = 0;
+        L = RankSmem(r.nbl, G, r.tie_warps, 0, 0, 0, r.kb);
+    }
     if (L.total > budget) return fail(HPDEX_ERR_UNSUPPORTED, "rank kernel layout does not fit");
     const size_t left = budget - L.total;
     r.gb = group_bytes(r.acc_in);
     r.cap = (int)std::min<size_t>(left / (r.kb + r.gb + 1), (size_t)1 << 30);  // + big-list entry share
     r.cap = std::max(0, r.cap - 8) & ~7;
-    L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.acc_in, r.cap, r.kb);
+    L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.cnt_in, r.cap, r.kb);
     while (L.total > budget && r.cap > 0) {  // the big list is sized for compact slabs
         r.cap = std::max(0, r.cap - 64);
-        L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.acc_in, r.cap, r.kb);
+        L = RankSmem(r.nbl, G, r.tie_warps, r.acc_in, r.cnt_in, r.cap, r.kb);
     }
     r.smem = L.total;
     int blocks = 0;
@@ -768,7 +785,7 @@ void set_layout_args(RankArgs& a, const RankLayout& r, int G, void* dk, void* dg
     a.nb_max_log2 = r.nbl;
     a.elem_smem_cap = r.cap;
     a.acc_in_smem = r.acc_in;
-    a.cnt_in_smem = r.acc_in;
+    a.cnt_in_smem = r.cnt_in;
     a.tie_warps = r.tie_warps;
 }
 
@@ -776,7 +793,7 @@ int configure_rank(hpdex_plan* p) {
     const hpdex_matrix* m = p->m;
     const int G = (int)p->G;
     RankLayout r;
-    TRY(rank_layout(m->dev, m->dtype, G, m->max_col_nnz, &r, p->nbl));
+    TRY(rank_layout(m->dev, m->dtype, G, m->max_col_nnz, &r, p->nbl, p->cnt_mode));
     p->rank_smem = r.smem;
     p->rank_grid = r.grid;
     TRY(p->dk.alloc(r.dk_bytes()));
@@ -1540,6 +1557,26 @@ int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits) {
     return st;
 }
 
+int hpdex_plan_set_run_counters(hpdex_plan* p, int32_t mode) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (mode < -1 || mode > 1) return fail(HPDEX_ERR_ARGUMENT, "run counter mode must be -1, 0 or 1");
+    if (mode == p->cnt_mode) return HPDEX_OK;
+    const int old = p->cnt_mode;
+    const RankArgs keep = p->ra;  // the plan's other launch settings stay as they were
+    p->cnt_mode = mode;
+    int st = configure_rank(p);
+    if (st != HPDEX_OK) {
+        p->cnt_mode = old;
+        configure_rank(p);
+    }
+    p->ra.erfc_table = keep.erfc_table;
+    p->ra.drain_wait = keep.drain_wait;
+    p->ra.no_histogram = keep.no_histogram;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }  // re-captured
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return st;
+}
+
 int hpdex_plan_set_histogram(hpdex_plan* p, int32_t on) {
     if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
     p->hist_on = on != 0;
@@ -1913,7 +1950,7 @@ int oneshot_pipelined(int32_t dtype, const void* data, const int64_t* indices, c
     // a scratch set of their own.
     cudaStream_t sc2 = r.comp2;
     RankLayout lay2;
-    TRY(rank_layout(m->dev, dtype, (int)p->G, m->max_col_nnz, &lay2, p->nbl));
+    TRY(rank_layout(m->dev, dtype, (int)p->G, m->max_col_nnz, &lay2, p->nbl, p->cnt_mode));
     DevBuf<unsigned char> dk2, dg2, ek2, eg2, acc2;
     DevBuf<uint32_t> cnt2;
     TRY(dk2.alloc(lay2.dk_bytes()));

@@ -113,7 +113,8 @@ struct RankArgs {
                                // holds 8 entries per thread)
     int32_t elem_smem_cap;     // elements that fit in shared memory
     int32_t acc_in_smem;       // accumulators and packed run counters in shared memory
-    int32_t cnt_in_smem;       // (equal to acc_in_smem; kept for the layout arithmetic)
+    int32_t cnt_in_smem;       // run counters in shared memory (with the accumulators; else in
+                               // global memory, and rounds resolve repeated groups by warp match)
     int32_t tie_warps;         // = warps per CTA (each owns packed run counters)
     const double* erfc_table;  // non-null: the kernel also computes the asymptotic p-values
                                // (P replaces the tie sums); null: a p-value kernel follows
@@ -377,8 +378,10 @@ __device__ __forceinline__ void add_pair(const Acc& acc, uint32_t g, unsigned lo
 // Buckets with more than one key take lt and c0 from broadcasting their (few) reference lanes.
 // s: the warp's group counters show which groups occur more than once in the round; such lanes
 // of one-key buckets match their group, those of other buckets compare pairwise among
-// themselves. `cnt` is zero on entry and on exit.
-template <class K, bool SH>
+// themselves. `cnt` is zero on entry and on exit. RM (the counters are in global memory, where
+// a round's increments, read-back and clear would cost more): one warp match over the target
+// lanes' groups instead of the counters.
+template <class K, bool SH, bool RM>
 __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, unsigned sub,
                                               uint32_t rb, const Acc& acc, uint32_t* cnt,
                                               unsigned long long& tref) {
@@ -402,23 +405,34 @@ __device__ __forceinline__ void resolve_round(bool active, K key, uint32_t g, un
             c0 += kj == key;
         }
     }
-    if (is_tar) cnt_inc<SH>(cnt, g);
-    __syncwarp();
-    uint32_t ng = 0;
-    if (is_tar) {
-        const uint32_t w = cnt[g >> 1];
-        ng = (g & 1u) ? (w >> 16) : (w & 0xffffu);
+    uint32_t s = 1, ng = 0;
+    bool repeats = true;  // (warp-uniform) some target group occurs more than once in the round
+    if constexpr (RM) {
+        // target lanes with this lane's group (other lanes match nobody: group ids are below 2^31)
+        const unsigned same = __match_any_sync(0xffffffffu, is_tar ? g : (0x80000000u | (threadIdx.x & 31u)));
+        ng = is_tar ? (uint32_t)__popc(same) : 0u;
+        if (ng > 1u && !mixed) s = (uint32_t)__popc(same & sub);
+    } else {
+        if (is_tar) cnt_inc<SH>(cnt, g);
+        __syncwarp();
+        if (is_tar) {
+            const uint32_t w = cnt[g >> 1];
+            ng = (g & 1u) ? (w >> 16) : (w & 0xffffu);
+        }
+        __syncwarp();
+        if (is_tar) cnt[g >> 1] = 0u;  // clears both groups of the word; both were read above
+        repeats = __ballot_sync(0xffffffffu, ng > 1u) != 0u;
+        if (repeats) {
+            // every lane of a one-key bucket whose group repeats in the round is in `one`, so
+            // the match over `one` sees all lanes of its bucket with its group
+            const unsigned one = __ballot_sync(0xffffffffu, ng > 1u && !mixed);
+            if (ng > 1u && !mixed) s = (uint32_t)__popc(__match_any_sync(one, g) & sub);
+        }
     }
-    __syncwarp();
-    if (is_tar) cnt[g >> 1] = 0u;  // clears both groups of the word; both were read above
-    const unsigned rep = __ballot_sync(0xffffffffu, ng > 1u);
-    uint32_t s = 1;
-    if (rep) {
-        // every lane of a one-key bucket whose group repeats in the round is in `one`, so the
-        // match over `one` sees all lanes of its bucket with its group
-        const unsigned one = __ballot_sync(0xffffffffu, ng > 1u && !mixed);
-        if (ng > 1u && !mixed) s = (uint32_t)__popc(__match_any_sync(one, g) & sub);
-        const unsigned many = rep & ~one;
+    if (repeats) {
+        // lanes of buckets with several keys whose group repeats: every lane with the same
+        // bucket, key and group is among them
+        const unsigned many = __ballot_sync(0xffffffffu, ng > 1u && mixed);
         if (many) {
             uint32_t c = 0;
             for (unsigned r = many; r; r &= r - 1u) {
@@ -603,7 +617,8 @@ __device__ __forceinline__ void pvalue_tiles(const RankTask* tk, int c, uint32_t
 // starting at `base` in the gene's bucket order (hall[b - 1] = start of bucket b).
 // Buckets of 2..32 elements are packed whole, in bucket order, into rounds of up to 32
 // lanes; `tbl` (32 bytes per warp) maps the k-th such bucket of a chunk to its lane.
-template <class K, bool SH, class EK, class EG>
+// RM: the run counters are in global memory (rounds by warp match, see resolve_round).
+template <class K, bool SH, bool RM, class EK, class EG>
 __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi, uint32_t base,
                           const uint32_t* hall, const uint32_t* href, uint32_t* biglist,
                           uint32_t biglist_cap, uint32_t* s_chunk, uint32_t* s_nbig,
@@ -618,7 +633,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
     auto resolve_listed = [&](uint32_t b) {
         const uint32_t sb = (b == blo) ? base : hall[b - 1];
         const uint32_t m = hall[b] - sb;
-        if (m <= 65535u) resolve_big<K, false, SH, SH>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
+        if (m <= 65535u) resolve_big<K, false, SH, SH && !RM>(sb - base, m, href[b], ek, eg, acc, cnt, tref);
         else resolve_big<K, true, SH, false>(sb - base, m, href[b], ek, eg, acc, wide_cnt, tref);
     };
     for (;;) {
@@ -680,7 +695,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
                     g = eg[sq + e];
                 }
                 const unsigned sub = (mq >= 32u ? 0xffffffffu : ((1u << mq) - 1u)) << pq;
-                resolve_round<K, SH>(active, key, g, sub, rq, acc, cnt, tref);
+                resolve_round<K, SH, RM>(active, key, g, sub, rq, acc, cnt, tref);
                 ord0 += __popc(I);
                 rem &= ~I;
             }
@@ -692,7 +707,7 @@ __device__ void rank_slab(const EK* ek, const EG* eg, uint32_t blo, uint32_t bhi
             const uint32_t mj = __shfl_sync(0xffffffffu, m, j);
             const uint32_t sj = __shfl_sync(0xffffffffu, s0, j);
             const uint32_t rj = __shfl_sync(0xffffffffu, rb, j);
-            if (mj <= 65535u) resolve_big<K, false, SH, SH>(sj, mj, rj, ek, eg, acc, cnt, tref);
+            if (mj <= 65535u) resolve_big<K, false, SH, SH && !RM>(sj, mj, rj, ek, eg, acc, cnt, tref);
             else resolve_big<K, true, SH, false>(sj, mj, rj, ek, eg, acc, wide_cnt, tref);
         }
     }
@@ -1041,7 +1056,9 @@ __device__ __forceinline__ void finalize_gene(const RankTask* tk, int c, int G, 
 // can hold small integers; without it the bucket path keeps its register allocation).
 // CPX: the variant that can compact its decoded copy (launched when a task of the launch asks
 // for it, RankTask::compact_decode).
-template <class V, int NT, bool ACC_SMEM, bool HIST, bool CPX>
+// RM: accumulators in shared memory, run counters in global memory (large G: the shared memory
+// goes to elements; rounds resolve repeated groups by warp match).
+template <class V, int NT, bool ACC_SMEM, bool HIST, bool CPX, bool RM>
 __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     using K = typename Val<V>::Key;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1065,7 +1082,8 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     const int wait_polls = a.drain_wait ? kDrainWaitIters : 0;
     const int GL = a.G;  // layout G
     const int NBMAX = 1 << a.nb_max_log2;
-    const RankSmem L(a.nb_max_log2, GL, a.tie_warps, ACC_SMEM, ACC_SMEM, a.elem_smem_cap,
+    constexpr bool CNT_SMEM = ACC_SMEM && !RM;
+    const RankSmem L(a.nb_max_log2, GL, a.tie_warps, ACC_SMEM, CNT_SMEM, a.elem_smem_cap,
                      (int)sizeof(K));
     const int cw = RankSmem::cnt_words(GL);
 
@@ -1081,7 +1099,7 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
     uint32_t* cnt_glob = a.cnt_global + cta * a.tie_warps * (cw + GL);
     if constexpr (ACC_SMEM) {
         accb = smem;
-        cnt_base = reinterpret_cast<uint32_t*>(smem + L.acc_bytes);
+        cnt_base = CNT_SMEM ? reinterpret_cast<uint32_t*>(smem + L.acc_bytes) : cnt_glob;
     } else {
         accb = a.acc_global + cta * 24 * GL;
         cnt_base = cnt_glob;
@@ -1425,17 +1443,17 @@ __global__ void __launch_bounds__(NT, 1) mwu_rank_kernel(const RankArgs a) {
 
             // ---- rank ----
             if (in_smem && compact)
-                rank_slab<uint32_t, ACC_SMEM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
+                rank_slab<uint32_t, ACC_SMEM, RM>(eo_s, ego_s, blo, bhi, base, hall, href, biglist,
                                               biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                               wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
                                               &s_pvq, a.erfc_table, wait_polls);
             else if (in_smem)
-                rank_slab<K, ACC_SMEM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
+                rank_slab<K, ACC_SMEM, RM>(ek_s, eg_s, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
                                        &s_pvq, a.erfc_table, wait_polls);
             else
-                rank_slab<K, ACC_SMEM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
+                rank_slab<K, ACC_SMEM, RM>(ek_g, eg_g, blo, bhi, base, hall, href, biglist,
                                        biglist_cap, &s_chunk, &s_nbig, &s_bigi, &s_wdone, acc, cnt,
                                        wide_cnt, s_tbl[warp], tref, slab ? nullptr : pv_tk, pv_c,
                                        &s_pvq, a.erfc_table, wait_polls);

@@ -9,10 +9,13 @@ namespace hpdex {
 
 cudaError_t HPDEX_CAT(rank_launch_, HPDEX_RANK_T)(const RankArgs& a, int grid, size_t smem,
                                                   cudaStream_t s) {
-    auto k = !a.acc_in_smem   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>
-             : !a.no_histogram ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>
-             : a.any_compact   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true>
-                               : mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false>;
+    // (accumulators in shared memory, histogram path, decoded-copy compaction, run counters in
+    // global memory)
+    auto k = !a.acc_in_smem   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true, false>
+             : !a.cnt_in_smem  ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true, true>
+             : !a.no_histogram ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true, false>
+             : a.any_compact   ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true, false>
+                               : mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false, false>;
     k<<<grid, 1024, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -20,13 +23,15 @@ cudaError_t HPDEX_CAT(rank_launch_, HPDEX_RANK_T)(const RankArgs& a, int grid, s
 cudaError_t HPDEX_CAT(rank_occupancy_, HPDEX_RANK_T)(size_t smem, size_t smem_optin,
                                                      int acc_in_smem, int* blocks) {
     // the variants of an accumulator layout get the same shared-memory limit
-    decltype(&mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>) ks[3] = {
-        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false>
-                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>,
-        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true>
-                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>,
-        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true>
-                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true>};
+    decltype(&mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true, false>) ks[4] = {
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, false, false>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true, false>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true, false>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true, false>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, true, true, false>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true, false>,
+        acc_in_smem ? mwu_rank_kernel<HPDEX_RANK_V, 1024, true, false, true, true>
+                    : mwu_rank_kernel<HPDEX_RANK_V, 1024, false, false, true, false>};
     for (auto k : ks) {
         cudaFuncAttributes fa;
         cudaError_t e = cudaFuncGetAttributes(&fa, k);

@@ -169,6 +169,12 @@ class Plan:
         every gene; the results are the same."""
         _lib.check(_lib.lib().hpdex_plan_set_histogram(self._h, int(bool(on))))
 
+    def set_run_counters(self, mode: int) -> None:
+        """Diagnostic: the rank kernel's per-warp run counters in shared memory (1), in global
+        memory (0, rounds by warp match) or placed automatically (-1, the default: shared up to
+        1,024 groups); results do not change."""
+        _lib.check(_lib.lib().hpdex_plan_set_run_counters(self._h, int(mode)))
+
     def set_drain_wait(self, on: bool) -> None:
         """Diagnostic: on makes a warp of the rank kernel wait a bounded number of polls for a
         large bucket another warp is still listing (off, the default, leaves it to the pass after

@@ -224,6 +224,12 @@ int hpdex_plan_download(hpdex_plan* p, double* U1_out, double* P_out);
  * gene's elements at the cost of larger buckets. The results do not depend on it. */
 int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits);
 
+/* Diagnostic. Where the rank kernel keeps its per-warp run counters (16 bits per group):
+ * mode 1 in shared memory (when the accumulators are there), 0 in global memory (its rounds
+ * then resolve repeated groups by warp match, and the shared memory goes to elements), -1 (the
+ * default) in shared memory up to 1,024 groups. The results are the same in every mode. */
+int hpdex_plan_set_run_counters(hpdex_plan* p, int32_t mode);
+
 /* The rank kernel takes each gene whose stored values are integers of magnitude below 2^31
  * (UMI counts) and whose value span times the number of groups fits its shared memory through
  * a histogram path: one counter per (value, group), rank sums from a prefix scan of the

@@ -165,3 +165,34 @@ def test_bucket_table_size_does_not_change_results():
         plan.close()
     finally:
         M.close()
+
+
+@pytest.mark.parametrize("n_targets", [12, 1200])
+def test_run_counter_placement_does_not_change_results(n_targets):
+    """The per-warp run counters in shared memory (rounds count repeated groups with them) or in
+    global memory (rounds match groups across the warp; big buckets count in global memory) give
+    the same doubles, on columns with tie-heavy, dominant-value and impure big buckets; with
+    1,200 targets the automatic placement is global memory, and it equals the oracle there."""
+    from hpdex_gb300.resident import BATCHED, ResidentMatrix
+    rng = np.random.default_rng(17)
+    if n_targets == 12:
+        sizes = [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]
+        w = _workload(3, 150_000, COLUMNS, 30_000, sizes)
+    else:
+        sizes = list(rng.integers(20, 90, size=n_targets))
+        w = _workload(5, 120_000, COLUMNS, 20_000, sizes)
+        assert _oracle_compare(w, zero_handling="min") == "ok"
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    try:
+        plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        plan.run(BATCHED)
+        U1a, Pa = plan.download()
+        for mode in (0, 1, -1):
+            plan.set_run_counters(mode)
+            plan.run(BATCHED)
+            U1b, Pb = plan.download()
+            np.testing.assert_array_equal(U1b, U1a)
+            np.testing.assert_array_equal(Pb, Pa)
+        plan.close()
+    finally:
+        M.close()
