@@ -94,14 +94,18 @@ def test_fused_large_columns():
 def test_fused_oversized_buckets_and_many_groups():
     """Columns above the shared-memory capacity with one dominant value (a bucket of more
     than 65,535 elements, ranked in place in global memory) and packed distinct keys; then
-    2,000 targets, where the accumulators live in global memory and group ids are 32-bit. The
-    fused plan equals the one-shot call (separate p-value kernel) bit for bit."""
+    2,000 targets (accumulators in shared memory, run counters in global memory) and 7,000
+    targets (accumulators in global memory too, 32-bit group ids). The fused plan equals the
+    one-shot call (separate p-value kernel) bit for bit."""
     from test_gpu_large_columns import COLUMNS, _workload
     from hpdex_gb300.backend.bin import kernel
     rng = np.random.default_rng(2)
     cases = [_workload(3, 150_000, COLUMNS, 30_000,
                        [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]),
-             _workload(5, 60_000, COLUMNS[:3], 8_000, list(rng.integers(20, 26, size=2_000)))]
+             _workload(5, 60_000, COLUMNS[:3], 8_000, list(rng.integers(20, 26, size=2_000))),
+             _workload(6, 45_000, COLUMNS[:3], 6_000, list(rng.integers(3, 7, size=7_000)))]
+    from test_gpu_parity import _oracle_compare
+    assert _oracle_compare(cases[-1], zero_handling="min") == "ok"
     for w in cases:
         U1, P = _fused_separate(w, zero_handling="min", use_continuity=True, fast_norm=False)
         U1o, Po = kernel.mannwhitneyu(w.data, w.indices, w.indptr, w.group_id, w.n_targets,
