@@ -443,7 +443,7 @@ struct hpdex_plan {
     int rank_grid = 0;
     // exact tables
     DevBuf<long long> pair_n1, pair_n2, pair_off, work_off;
-    DevBuf<double> tables;
+    DevBuf<double> tables, pair_recip;
     DevBuf<unsigned long long> work;
     DevBuf<int32_t> pair_of_target, pair_of_test;
     DevBuf<unsigned char> pair_mark;  // zero_handling none: (n1, n2) cells present
@@ -956,6 +956,10 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
         else
             exact_reference_table_kernel<256><<<np, 256, 0, s>>>(et);
         CUDA_TRY(cudaGetLastError());
+        TRY(p->pair_recip.alloc((size_t)np));
+        exact_recip_kernel<<<(np + 255) / 256, 256, 0, s>>>(p->pair_n1.p, p->pair_n2.p, p->pair_off.p,
+                                                            p->tables.p, np, p->pair_recip.p);
+        CUDA_TRY(cudaGetLastError());
     }
     ExactArgs a{};
     a.U1 = p->U1.p;
@@ -977,6 +981,7 @@ int run_exact(hpdex_plan* p, cudaStream_t s) {
     a.pair_n2 = p->pair_n2.p;
     a.offset = p->pair_off.p;
     a.tables = p->tables.p;
+    a.recip = p->pair_recip.p;
     const int grid = (int)std::min<long long>((n + 255) / 256, (long long)p->m->dev.sms * 8);
     mwu_pvalue_exact_kernel<<<grid, 256, 0, s>>>(a);
     CUDA_TRY(cudaGetLastError());

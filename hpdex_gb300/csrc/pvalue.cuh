@@ -336,10 +336,27 @@ struct ExactArgs {
     const long long* pair_n2;
     const long long* offset;
     const double* tables;
+    const double* recip;            // [n_pairs] RN(1 / total) of each table, 0 where the
+                                    // quotients must take an IEEE division (total 0 or not finite)
 };
 
-// survival P(U >= floor(U)) from a table, the reference's formula (:160-179)
-__device__ __forceinline__ double table_sf(const double* pmf, long long umax, double U) {
+// RN(1 / total) of each table (total = prefix[n1*n2]), for its quotients by the total: the
+// numerators are counts (0 or at least 1), so with 1 <= total < 2^960 no quotient leaves the
+// normal range and Markstein's division (div_by_recip) gives the IEEE quotient. A total of 0 (the
+// reference variant's wrapping counts) or beyond keeps the IEEE division.
+__global__ void exact_recip_kernel(const long long* pair_n1, const long long* pair_n2,
+                                   const long long* offset, const double* tables, int32_t n_pairs,
+                                   double* recip) {
+    for (int pi = blockIdx.x * blockDim.x + threadIdx.x; pi < n_pairs; pi += gridDim.x * blockDim.x) {
+        const long long umax = pair_n1[pi] * pair_n2[pi];
+        const double total = tables[offset[pi] + 2 * umax + 1];
+        recip[pi] = (total >= 1.0 && total < 0x1p960) ? __drcp_rn(total) : 0.0;
+    }
+}
+
+// survival P(U >= floor(U)) from a table, the reference's formula (:160-179); y = RN(1 / total)
+// or 0 (IEEE division)
+__device__ __forceinline__ double table_sf(const double* pmf, long long umax, double U, double y) {
     if (umax == 0) return 1.0;
     const double* pre = pmf + (umax + 1);
     double Uc = U < 0.0 ? 0.0 : U;
@@ -350,19 +367,25 @@ __device__ __forceinline__ double table_sf(const double* pmf, long long umax, do
     const long long small = u_stat < kc ? u_stat : kc;
     const double cdf_small = pre[small];
     const double pmf_small = pmf[small];
+    auto quot = [&](double x) { return y != 0.0 ? div_by_recip(x, total, y) : __ddiv_rn(x, total); };
     if (u_stat <= kc)
-        return __dadd_rn(__dsub_rn(1.0, __ddiv_rn(cdf_small, total)), __ddiv_rn(pmf_small, total));
-    return __ddiv_rn(cdf_small, total);
+        return __dadd_rn(__dsub_rn(1.0, quot(cdf_small)), quot(pmf_small));
+    return quot(cdf_small);
 }
 
 // zero_handling none: marks the (n1, n2) cells of a dense H x W map that occur among the tests
-// (sample sizes outside the map only come with duplicate row ids, which the run reports)
+// (sample sizes outside the map only come with duplicate row ids, which the run reports). Few
+// cells are marked by many tests: a test stores only while its cell still reads 0, so the stores
+// to one cell do not queue up (every store writes the same 1).
 __global__ void exact_mark_pairs_kernel(const uint32_t* n1g, const uint32_t* n2t, long long n,
                                         int32_t n_cols, int32_t H, int32_t W, unsigned char* mark) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint32_t n1 = n1g[i % n_cols], n2 = n2t[i];
-        if (n1 < (uint32_t)H && n2 < (uint32_t)W) mark[(size_t)n1 * W + n2] = 1;
+        if (n1 < (uint32_t)H && n2 < (uint32_t)W) {
+            unsigned char* m = mark + (size_t)n1 * W + n2;
+            if (__ldcg(m) == 0) *m = 1;
+        }
     }
 }
 
@@ -396,7 +419,7 @@ __global__ void mwu_pvalue_exact_kernel(const ExactArgs a) {
             } else {
                 U = __dsub_rn(nprod, U1);
             }
-            const double sf = table_sf(pmf, umax, U);
+            const double sf = table_sf(pmf, umax, U, a.recip[pi]);
             p = (a.alternative == ALT_TWO_SIDED) ? __dmul_rn(2.0, sf) : sf;
             if (p < 0.0) p = 0.0;
             if (p > 1.0) p = 1.0;
