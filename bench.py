@@ -19,10 +19,13 @@ One step = one DE call: per-(gene, target) U1 and P for all 500 x 8,000 tests.
   plain : the same plan in the plain form: one single-CTA launch per gene in column order, no
           graph, no queue; the launches go round-robin to up to 128 concurrent streams, so the
           comparison measures the queue and the graph, not idle SMs.
+  autotune: the plan's layout tuner (run counters in shared or global memory x bucket table of
+          2^13 or 2^12 entries, each candidate timed over 3 batched runs, the fastest kept);
+          also on the exact-mode plan, where 1,501 groups make the other choice.
   umi_counts: the 50,000 x 2,000 integer-count workload (49 targets): batched plan with the
           per-gene histogram path against the bucket path only, group means, CPU port.
   exact : the 60,000 x 4,000 dense exact-mode workload (40 reference cells, 1,500 targets):
-          both DP variants on the device, CPU port on a gene sample.
+          both DP variants on the device, the layout tuner, CPU port on a gene sample.
   serving: the serving loop (hpdex_gb300.serving) over five resident matrices (the
           200k x 8k screen, a 50k x 2k log1p-CP10k matrix, a 50k x 2k integer-count matrix,
           and a 1M x 20k log1p-CP10k atlas of 1e9 entries generated on the GPU with its
@@ -492,6 +495,8 @@ def exact_leg(steps=3):
             tt.append(t)
             rk.append(r)
             tb.append(p)
+        if variant == "reference":  # the layout tuner on this plan (1,501 groups)
+            out["autotune"] = plan.autotune(reps=3)
         plan.close()
         out[variant] = {"value": tests / (statistics.median(tt) / 1e3), "unit": UNIT,
                         "ms_per_step": statistics.median(tt), "rank_ms": statistics.median(rk),
@@ -604,6 +609,11 @@ def run_ours(args, rank, world):
     U1p, Pp = plan.download()
     same = bool(np.array_equal(U1p, U1) and np.array_equal(Pp, P))
 
+    # the layout tuner on the same plan: each candidate layout timed, the fastest kept
+    tuned = plan.autotune(reps=3)
+    U1t, Pt = plan.download()
+    tuned["results_identical"] = bool(np.array_equal(U1t, U1) and np.array_equal(Pt, P))
+
     # end to end through the public call: host arrays in, host arrays out
     h2d = w.nnz * (w.data.itemsize + 8) + 8 * (C + 1) + 4 * w.n_rows
     d2h = 2 * 8 * tests
@@ -688,6 +698,7 @@ def run_ours(args, rank, world):
                   "wall_ms": plain_wall * 1e3, "launches": pl,
                   "batched_speedup": (tests / elapsed_dev * args.steps) / (tests / (ptot / 1e3)),
                   "results_identical": same},
+        "autotune": tuned,
         "kernels_ms": {"rank_with_fused_pvalues": statistics.mean(rank_ms),
                        "separate_form": {"rank": min(x[1] for x in sep),
                                          "pvalue": min(x[2] for x in sep),

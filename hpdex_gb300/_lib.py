@@ -97,6 +97,8 @@ EXPORTS = {
     "hpdex_plan_set_fused_pvalues": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_set_drain_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_set_run_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "hpdex_plan_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
     "hpdex_plan_set_histogram": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_set_bucket_bits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "hpdex_plan_timings": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),

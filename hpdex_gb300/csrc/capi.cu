@@ -1525,6 +1525,40 @@ int hpdex_plan_run(hpdex_plan* p, int32_t mode) {
     return check_device_errors(p);
 }
 
+int hpdex_plan_autotune(hpdex_plan* p, int32_t reps, int32_t* run_counters_out,
+                        int32_t* bucket_bits_out, float* ms_out) {
+    if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
+    if (reps < 1) return fail(HPDEX_ERR_ARGUMENT, "reps must be >= 1");
+    // candidate layouts: run counters in shared / global memory x bucket table 2^13 / 2^12; each
+    // gives the same results, so the fastest (mean CUDA-event time of `reps` batched runs after
+    // one untimed run) is kept
+    const int32_t modes[2] = {1, 0}, bits[2] = {13, 12};
+    float best = 0.0f;
+    int32_t best_mode = 1, best_bits = 13;
+    for (int k = 0; k < 4; ++k) {
+        TRY(hpdex_plan_set_run_counters(p, modes[k / 2]));
+        TRY(hpdex_plan_set_bucket_bits(p, bits[k % 2]));
+        TRY(hpdex_plan_run(p, HPDEX_MODE_BATCHED));
+        float total = 0.0f;
+        for (int r = 0; r < reps; ++r) {
+            TRY(hpdex_plan_run(p, HPDEX_MODE_BATCHED));
+            total += p->last_ms[0];
+        }
+        const float ms = total / (float)reps;
+        if (ms_out) ms_out[k] = ms;
+        if (k == 0 || ms < best) {
+            best = ms;
+            best_mode = modes[k / 2];
+            best_bits = bits[k % 2];
+        }
+    }
+    TRY(hpdex_plan_set_run_counters(p, best_mode));
+    TRY(hpdex_plan_set_bucket_bits(p, best_bits));
+    if (run_counters_out) *run_counters_out = best_mode;
+    if (bucket_bits_out) *bucket_bits_out = best_bits;
+    return HPDEX_OK;
+}
+
 int hpdex_plan_set_fused_pvalues(hpdex_plan* p, int32_t on) {
     if (!p) return fail(HPDEX_ERR_ARGUMENT, "plan is NULL");
     if (p->opt.method != HPDEX_ASYMPTOTIC) {

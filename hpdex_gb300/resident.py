@@ -175,6 +175,19 @@ class Plan:
         1,024 groups); results do not change."""
         _lib.check(_lib.lib().hpdex_plan_set_run_counters(self._h, int(mode)))
 
+    def autotune(self, reps: int = 3) -> dict:
+        """Times the plan under each candidate rank-kernel layout (run counters in shared or
+        global memory, bucket table of 2^13 or 2^12 entries) and keeps the fastest; results do
+        not change. Returns the choice and the mean time of every candidate."""
+        mode, bits = ctypes.c_int32(), ctypes.c_int32()
+        ms = (ctypes.c_float * 4)()
+        _lib.check(_lib.lib().hpdex_plan_autotune(self._h, int(reps), ctypes.byref(mode),
+                                                  ctypes.byref(bits), ms))
+        names = [("shared", 13), ("shared", 12), ("global", 13), ("global", 12)]
+        return {"run_counters": "shared" if mode.value == 1 else "global",
+                "bucket_bits": bits.value,
+                "ms": {f"{c}/2^{b}": round(float(t), 4) for (c, b), t in zip(names, ms)}}
+
     def set_drain_wait(self, on: bool) -> None:
         """Diagnostic: on makes a warp of the rank kernel wait a bounded number of polls for a
         large bucket another warp is still listing (off, the default, leaves it to the pass after

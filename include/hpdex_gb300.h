@@ -230,6 +230,14 @@ int hpdex_plan_set_bucket_bits(hpdex_plan* p, int32_t bits);
  * default) in shared memory up to 1,024 groups. The results are the same in every mode. */
 int hpdex_plan_set_run_counters(hpdex_plan* p, int32_t mode);
 
+/* Measures the plan under each candidate layout of the rank kernel -- run counters in shared
+ * (1) or global (0) memory, bucket table of 2^13 or 2^12 entries -- as the mean CUDA-event time
+ * of `reps` batched runs after one untimed run, and keeps the fastest. All candidates give the
+ * same results. Outputs (each may be NULL): the chosen run-counter mode and bucket bits, and
+ * the four mean times in ms in the order (1, 13), (1, 12), (0, 13), (0, 12). */
+int hpdex_plan_autotune(hpdex_plan* p, int32_t reps, int32_t* run_counters_out,
+                        int32_t* bucket_bits_out, float* ms_out);
+
 /* The rank kernel takes each gene whose stored values are integers of magnitude below 2^31
  * (UMI counts) and whose value span times the number of groups fits its shared memory through
  * a histogram path: one counter per (value, group), rank sums from a prefix scan of the

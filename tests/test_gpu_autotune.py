@@ -1,0 +1,35 @@
+"""GPU: the plan's layout tuner times every candidate rank-kernel layout (run counters in shared
+or global memory, bucket table of 2^13 or 2^12 entries), keeps the fastest and leaves the
+results unchanged, bit for bit."""
+import numpy as np
+import pytest
+
+from test_gpu_large_columns import COLUMNS, _workload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n_targets", [12, 1200])
+def test_autotune_keeps_the_fastest_layout_and_the_results(n_targets):
+    from hpdex_gb300.resident import BATCHED, ResidentMatrix
+    rng = np.random.default_rng(23)
+    sizes = list(rng.integers(20, 90, size=n_targets)) if n_targets > 12 else \
+        [500, 800, 1200, 2000, 3000, 4500, 6000, 700, 650, 5200, 900, 3300]
+    w = _workload(7, 120_000, COLUMNS, 20_000, sizes)
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    try:
+        plan = M.plan(w.group_id, w.n_targets, zero_handling="min", use_continuity=True)
+        plan.run(BATCHED)
+        U1a, Pa = plan.download()
+        tuned = plan.autotune(reps=2)
+        assert tuned["run_counters"] in ("shared", "global") and tuned["bucket_bits"] in (12, 13)
+        ms = tuned["ms"]
+        assert len(ms) == 4 and all(t > 0.0 for t in ms.values())
+        assert ms[f"{tuned['run_counters']}/2^{tuned['bucket_bits']}"] == min(ms.values())
+        plan.run(BATCHED)  # the kept layout
+        U1b, Pb = plan.download()
+        np.testing.assert_array_equal(U1b, U1a)
+        np.testing.assert_array_equal(Pb, Pa)
+        plan.close()
+    finally:
+        M.close()
