@@ -1533,17 +1533,20 @@ int hpdex_plan_autotune(hpdex_plan* p, int32_t reps, int32_t* run_counters_out,
     // gives the same results, so the fastest (mean CUDA-event time of `reps` batched runs after
     // one untimed run) is kept
     const int32_t modes[2] = {1, 0}, bits[2] = {13, 12};
+    const int32_t old_mode = p->cnt_mode, old_bits = p->nbl;
     float best = 0.0f;
     int32_t best_mode = 1, best_bits = 13;
-    for (int k = 0; k < 4; ++k) {
-        TRY(hpdex_plan_set_run_counters(p, modes[k / 2]));
-        TRY(hpdex_plan_set_bucket_bits(p, bits[k % 2]));
-        TRY(hpdex_plan_run(p, HPDEX_MODE_BATCHED));
+    int st = HPDEX_OK;
+    for (int k = 0; k < 4 && st == HPDEX_OK; ++k) {
+        st = hpdex_plan_set_run_counters(p, modes[k / 2]);
+        if (st == HPDEX_OK) st = hpdex_plan_set_bucket_bits(p, bits[k % 2]);
+        if (st == HPDEX_OK) st = hpdex_plan_run(p, HPDEX_MODE_BATCHED);
         float total = 0.0f;
-        for (int r = 0; r < reps; ++r) {
-            TRY(hpdex_plan_run(p, HPDEX_MODE_BATCHED));
+        for (int r = 0; r < reps && st == HPDEX_OK; ++r) {
+            st = hpdex_plan_run(p, HPDEX_MODE_BATCHED);
             total += p->last_ms[0];
         }
+        if (st != HPDEX_OK) break;
         const float ms = total / (float)reps;
         if (ms_out) ms_out[k] = ms;
         if (k == 0 || ms < best) {
@@ -1551,6 +1554,12 @@ int hpdex_plan_autotune(hpdex_plan* p, int32_t reps, int32_t* run_counters_out,
             best_mode = modes[k / 2];
             best_bits = bits[k % 2];
         }
+    }
+    if (st != HPDEX_OK) {  // the plan keeps the layout it had (the error stays the one reported)
+        const std::string msg = hpdex_last_error();
+        hpdex_plan_set_run_counters(p, old_mode);
+        hpdex_plan_set_bucket_bits(p, old_bits);
+        return fail(st, "%s", msg.c_str());
     }
     TRY(hpdex_plan_set_run_counters(p, best_mode));
     TRY(hpdex_plan_set_bucket_bits(p, best_bits));

@@ -33,3 +33,26 @@ def test_autotune_keeps_the_fastest_layout_and_the_results(n_targets):
         plan.close()
     finally:
         M.close()
+
+
+def test_autotune_reports_the_plans_error():
+    """A plan whose runs fail (a reference of 3 cells under zero_handling=none: most genes store
+    fewer than 2 of them) makes the tuner raise the run's error, as a run would."""
+    from hpdex_gb300.resident import BATCHED, ResidentMatrix
+    from hpdex_gb300 import synthetic
+    w = synthetic.umi_counts(seed=42, n_rows=8_000, n_cols=50, n_targets=5)
+    gid = np.full(w.n_rows, -1, np.int32)
+    gid[:3] = 0
+    gid[3:6] = 1
+    M = ResidentMatrix(w.data, w.indices, w.indptr, w.n_rows)
+    try:
+        plan = M.plan(gid, 1, zero_handling="none")
+        with pytest.raises(RuntimeError) as e_run:
+            plan.run(BATCHED)
+        with pytest.raises(RuntimeError) as e_tune:
+            plan.autotune(reps=1)
+        assert str(e_tune.value) == str(e_run.value)
+        assert "Sample too small" in str(e_tune.value)
+        plan.close()
+    finally:
+        M.close()
