@@ -937,26 +937,32 @@ static __device__ __noinline__ unsigned long long hist_gene(
     const int words = (int)hist_words(hVp, G);
     for (int i = 4 * tid; i < words; i += 4 * NT)
         *reinterpret_cast<uint4*>(hc + i) = make_uint4(0u, 0u, 0u, 0u);
-    // the previous gene's p-values: as on the bucket path, some warps start on them
-    if (pv_tk && warp < kPvWarps) pvalue_tiles(pv_tk, pv_c, s_pvq, erfc_table);
     __syncthreads();
+    // the previous gene's p-values: one warp per pending tile (at most kPvWarps) takes them
+    // while the other warps count, as on the bucket path (a barrier between the two would make
+    // every warp wait for the tiles' FP64 chains)
+    const int pvw = pv_tk ? min(kPvWarps, (pv_tk->G + 30) / 32) : 0;
+    if (warp < pvw) {
+        pvalue_tiles(pv_tk, pv_c, s_pvq, erfc_table);
+    } else {
     // one streaming pass: each stored element increments its (value, group) counter; the row
     // ids and values of the next four elements are in flight while the current ones' group ids
-    // are gathered and counted
+    // are gathered and counted (the counting threads are those of warps pvw..)
+    const uint32_t nthr = (uint32_t)(NT - 32 * pvw), t0 = (uint32_t)(tid - 32 * pvw);
     int32_t r[4];
     V v[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const uint32_t e = (uint32_t)tid + (uint32_t)(k * NT);
+        const uint32_t e = t0 + (uint32_t)k * nthr;
         r[k] = e < nraw ? __ldcs(rows + e) : -1;
         v[k] = e < nraw ? ld_stream(data + e) : V(0);
     }
-    for (uint32_t i = (uint32_t)tid; i < nraw; i += 4u * NT) {
+    for (uint32_t i = t0; i < nraw; i += 4u * nthr) {
         int32_t rn[4];
         V vn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t e = i + 4u * NT + (uint32_t)(k * NT);
+            const uint32_t e = i + 4u * nthr + (uint32_t)k * nthr;
             rn[k] = e < nraw ? __ldcs(rows + e) : -1;
             vn[k] = e < nraw ? ld_stream(data + e) : V(0);
         }
@@ -976,6 +982,7 @@ static __device__ __noinline__ unsigned long long hist_gene(
 #pragma unroll
         for (int k = 0; k < 4; ++k) { r[k] = rn[k]; v[k] = vn[k]; }
     }
+    }  // counting warps
     __syncthreads();
     block_scan1<NT>(hc, hV, ws);  // hc[v] = reference elements below v, hc[V] = all of them
     // one warp per target group: its row against the reference's prefix counts
